@@ -1,0 +1,611 @@
+// C ABI of the library (include/geon_gpu.h): handles, host<->device staging,
+// launches and status mapping. Host arithmetic here that must match the
+// reference (the bisection midpoints, camera constants) is compiled with
+// -ffp-contract=off.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace geon;
+
+struct geon_metric {
+  MetricDesc desc;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<int> g_show_stars{1};
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(e == cudaErrorMemoryAllocation ? GEON_ERR_OOM : GEON_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define GEON_CUDA(call)                                  \
+  do {                                                   \
+    cudaError_t e__ = (call);                            \
+    if (e__ != cudaSuccess) return cuda_fail(e__, #call); \
+  } while (0)
+
+// Stream-ordered device buffer freed when it leaves scope.
+struct DBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  cudaError_t alloc(size_t bytes, cudaStream_t st) {
+    s = st;
+    if (bytes == 0) bytes = 16;
+    return cudaMallocAsync(&p, bytes, st);
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+constexpr double RADS_PER_DEG = 3.141592653589793 / 180.0;  // f64::to_radians
+
+cudaStream_t host_stream() { return cudaStreamPerThread; }
+
+int check_metric(geon_metric_t m) {
+  if (!m) return fail(GEON_ERR_INVALID, "null metric handle");
+  return GEON_OK;
+}
+
+int sync_and_flags(cudaStream_t s, const int* d_flags, int* h_flags) {
+  GEON_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  GEON_CUDA(cudaGetLastError());
+  return GEON_OK;
+}
+
+int singular_status(int flags) {
+  if (flags & 1) return fail(GEON_ERR_SINGULAR_METRIC, "metric became singular - coordinate chart broke down");
+  return GEON_OK;
+}
+
+// Build the device camera for a metric: the tetrad comes from the device (same
+// functor as the trace), the image-plane constants from the host libm.
+int make_camera(geon_metric_t m, const geon_camera* cam, int64_t spa, CameraDesc& c, cudaStream_t s) {
+  if (!cam || cam->width <= 0 || cam->height <= 0) return fail(GEON_ERR_INVALID, "bad camera size");
+  if (cam->forward_sign != 1 && cam->forward_sign != -1) return fail(GEON_ERR_INVALID, "forward_sign must be +1 or -1");
+  DBuf d;
+  GEON_CUDA(d.alloc(sizeof(double) * 20 + sizeof(int), s));
+  double* d_obs = d.as<double>();
+  double* d_tet = d_obs + 4;
+  int* d_status = reinterpret_cast<int*>(d_obs + 20);
+  GEON_CUDA(cudaMemcpyAsync(d_obs, cam->observer, sizeof(double) * 4, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(launch_tetrad(m->desc, d_obs, d_tet, d_status, s));
+  double tet[16];
+  int status = 0;
+  GEON_CUDA(cudaMemcpyAsync(tet, d_tet, sizeof tet, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaMemcpyAsync(&status, d_status, sizeof status, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  if (status == GEON_ERR_NOT_TIMELIKE) return fail(status, "observer is not in a timelike region (g_tt >= 0)");
+  if (status == GEON_ERR_GRAM_SCHMIDT) return fail(status, "Gram-Schmidt produced non-spacelike vector - chart broken at this point");
+  std::memcpy(c.tet, tet, sizeof tet);
+  std::memcpy(c.obs, cam->observer, sizeof c.obs);
+  const double fov = cam->fov_y_deg * RADS_PER_DEG;
+  const double aspect = (double)cam->width / (double)cam->height;
+  c.h_img = std::tan(fov * 0.5);
+  c.w_img = c.h_img * aspect;
+  c.width_d = (double)cam->width;
+  c.height_d = (double)cam->height;
+  c.width = cam->width;
+  c.height = cam->height;
+  c.spa = spa < 1 ? 1 : spa;
+  c.inv_spa = 1.0 / (double)c.spa;
+  c.forward_sign = cam->forward_sign;
+  return GEON_OK;
+}
+
+TraceLaunch base_launch(geon_metric_t m, double step, int64_t max_steps) {
+  TraceLaunch L;
+  std::memset(&L, 0, sizeof L);
+  L.M = m->desc;
+  L.step = step;
+  L.half_step = 0.5 * step;
+  L.sixth = step / 6.0;
+  L.max_steps = max_steps;
+  return L;
+}
+
+int copy_out(void* host, const void* dev, size_t bytes, cudaStream_t s) {
+  if (host && bytes) GEON_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s));
+  return GEON_OK;
+}
+
+}  // namespace
+
+// Kernels defined in trace_fp64.cu used only from here.
+namespace geon {
+cudaError_t launch_camera_rays(const CameraDesc& c, double du, double dv, double* out, cudaStream_t s);
+cudaError_t launch_equatorial_rays(double m, double r_obs, const double* alpha, int64_t n, double* out,
+                                   cudaStream_t s);
+}  // namespace geon
+
+extern "C" {
+
+const char* geon_version(void) { return "geon-gb300 0.1 (sm_103a)"; }
+
+const char* geon_last_error(void) { return g_last_error.c_str(); }
+
+void geon_render_config_default(geon_render_config* cfg) {
+  if (!cfg) return;
+  cfg->step = 0.05;
+  cfg->max_steps = 20000;
+  cfg->captured_rgb[0] = cfg->captured_rgb[1] = cfg->captured_rgb[2] = 0.0f;
+  cfg->diverged_rgb[0] = 1.0f;
+  cfg->diverged_rgb[1] = 0.0f;
+  cfg->diverged_rgb[2] = 1.0f;
+  cfg->samples_per_axis = 1;
+  cfg->show_stars = -1;
+  cfg->precision = GEON_FP64;
+}
+
+void geon_set_show_stars(int on) { g_show_stars.store(on ? 1 : 0); }
+int geon_get_show_stars(void) { return g_show_stars.load(); }
+
+int geon_metric_create(int kind, const double* params, int nparams, geon_metric_t* out) {
+  if (!out) return fail(GEON_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (kind < GEON_MINKOWSKI || kind > GEON_MORRIS_THORNE) return fail(GEON_ERR_INVALID, "unknown metric kind");
+  if (nparams < 0 || (nparams > 0 && !params)) return fail(GEON_ERR_INVALID, "bad params");
+  MetricDesc d;
+  std::memset(&d, 0, sizeof d);
+  d.kind = kind;
+  // Reference defaults: Schwarzschild::new (schwarzschild.rs:20-28), Alcubierre::default
+  // (alcubierre.rs:21-30), MorrisThorne::default (morris_thorne.rs:15-18).
+  static const double defaults[4][4] = {{0, 0, 0, 0}, {1.0, 1.001, 1000.0, 0}, {2.0, 0.5, 2.0, 0.0}, {1.0, 0, 0, 0}};
+  static const int counts[4] = {0, 3, 4, 1};
+  if (nparams > counts[kind]) return fail(GEON_ERR_INVALID, "too many params for this metric");
+  for (int i = 0; i < 4; ++i) d.p[i] = i < nparams ? params[i] : defaults[kind][i];
+  if (kind == GEON_SCHWARZSCHILD) {
+    d.capture_r = d.p[1] * 2.0 * d.p[0];
+    d.escape_r = d.p[2] * d.p[0];
+  }
+  if (kind == GEON_ALCUBIERRE) {
+    cudaStream_t s = host_stream();
+    DBuf b;
+    GEON_CUDA(b.alloc(sizeof(MetricDesc), s));
+    GEON_CUDA(cudaMemcpyAsync(b.p, &d, sizeof d, cudaMemcpyHostToDevice, s));
+    GEON_CUDA(launch_metric_init(b.as<MetricDesc>(), s));
+    GEON_CUDA(cudaMemcpyAsync(&d, b.p, sizeof d, cudaMemcpyDeviceToHost, s));
+    GEON_CUDA(cudaStreamSynchronize(s));
+  }
+  geon_metric* m = new (std::nothrow) geon_metric;
+  if (!m) return fail(GEON_ERR_OOM, "out of host memory");
+  m->desc = d;
+  *out = m;
+  return GEON_OK;
+}
+
+int geon_metric_destroy(geon_metric_t m) {
+  delete m;
+  return GEON_OK;
+}
+
+int geon_metric_kind(geon_metric_t m) { return m ? m->desc.kind : GEON_ERR_INVALID; }
+
+const char* geon_metric_name(geon_metric_t m) {
+  static const char* names[4] = {"minkowski", "schwarzschild", "alcubierre", "morris_thorne"};
+  return m ? names[m->desc.kind] : "";
+}
+
+static int pointwise(geon_metric_t m, int what, const double* in, size_t n, int in_width, double* out,
+                     int out_width, int32_t* iout) {
+  if (int rc = check_metric(m)) return rc;
+  if (n == 0) return GEON_OK;
+  if (!in || (!out && !iout)) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf din, dout, dflags;
+  GEON_CUDA(din.alloc(sizeof(double) * n * in_width, s));
+  GEON_CUDA(dout.alloc(out ? sizeof(double) * n * out_width : sizeof(int32_t) * n, s));
+  GEON_CUDA(dflags.alloc(sizeof(int), s));
+  GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
+  GEON_CUDA(cudaMemcpyAsync(din.p, in, sizeof(double) * n * in_width, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(launch_pointwise(m->desc, what, din.as<double>(), (int64_t)n, out ? dout.as<double>() : nullptr,
+                             out ? nullptr : dout.as<int32_t>(), dflags.as<int>(), s));
+  if (out) GEON_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double) * n * out_width, cudaMemcpyDeviceToHost, s));
+  else GEON_CUDA(cudaMemcpyAsync(iout, dout.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  int flags = 0;
+  if (int rc = sync_and_flags(s, dflags.as<int>(), &flags)) return rc;
+  return singular_status(flags);
+}
+
+int geon_metric_g(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_G, x, n, 4, out, 16, nullptr); }
+int geon_metric_dg(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_DG, x, n, 4, out, 64, nullptr); }
+int geon_metric_g_inv(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_GINV, x, n, 4, out, 16, nullptr); }
+int geon_metric_christoffel(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_CHRISTOFFEL, x, n, 4, out, 64, nullptr); }
+int geon_metric_terminate(geon_metric_t m, const double* x, size_t n, int32_t* out) { return pointwise(m, PW_TERMINATE, x, n, 4, nullptr, 0, out); }
+int geon_metric_asymptotic_direction(geon_metric_t m, const double* st, size_t n, double* out) { return pointwise(m, PW_ASYM, st, n, 8, out, 3, nullptr); }
+
+int geon_trace_dev(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps, int precision,
+                   int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual,
+                   void* stream) {
+  if (int rc = check_metric(m)) return rc;
+  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (n == 0) return GEON_OK;
+  if (!y0 || !term || !final_state || !steps_taken || !null_residual)
+    return fail(GEON_ERR_INVALID, "geon_trace_dev needs every device buffer");
+  if (max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DBuf ws;
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) + sizeof(int) * 2, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) + sizeof(int) * 2, s));
+  TraceLaunch L = base_launch(m, step, max_steps);
+  L.n = (int64_t)n;
+  L.y0 = y0;
+  L.term = term;
+  L.yfinal = final_state;
+  L.steps = steps_taken;
+  L.resid = null_residual;
+  L.queue = ws.as<unsigned long long>();
+  L.flags = reinterpret_cast<int*>(L.queue + 1);
+  GEON_CUDA(launch_trace_fp64(L, SRC_ARRAY, SINK_TRACE, s));
+  return GEON_OK;
+}
+
+int geon_trace(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps, int precision,
+               int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual) {
+  if (int rc = check_metric(m)) return rc;
+  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (n == 0) return GEON_OK;
+  if (!y0 || !term) return fail(GEON_ERR_INVALID, "null buffer");
+  if (max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
+  cudaStream_t s = host_stream();
+  DBuf dy0, dterm, dyf, dsteps, dres, ws;
+  GEON_CUDA(dy0.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(dterm.alloc(sizeof(int32_t) * n, s));
+  GEON_CUDA(dyf.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(dsteps.alloc(sizeof(int64_t) * n, s));
+  GEON_CUDA(dres.alloc(sizeof(double) * n, s));
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) + sizeof(int) * 2, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) + sizeof(int) * 2, s));
+  GEON_CUDA(cudaMemcpyAsync(dy0.p, y0, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, s));
+  TraceLaunch L = base_launch(m, step, max_steps);
+  L.n = (int64_t)n;
+  L.y0 = dy0.as<double>();
+  L.term = dterm.as<int32_t>();
+  L.yfinal = dyf.as<double>();
+  L.steps = dsteps.as<int64_t>();
+  L.resid = dres.as<double>();
+  L.queue = ws.as<unsigned long long>();
+  L.flags = reinterpret_cast<int*>(L.queue + 1);
+  GEON_CUDA(launch_trace_fp64(L, SRC_ARRAY, SINK_TRACE, s));
+  if (int rc = copy_out(term, dterm.p, sizeof(int32_t) * n, s)) return rc;
+  if (int rc = copy_out(final_state, dyf.p, sizeof(double) * 8 * n, s)) return rc;
+  if (int rc = copy_out(steps_taken, dsteps.p, sizeof(int64_t) * n, s)) return rc;
+  if (int rc = copy_out(null_residual, dres.p, sizeof(double) * n, s)) return rc;
+  int flags = 0;
+  if (int rc = sync_and_flags(s, L.flags, &flags)) return rc;
+  return singular_status(flags);
+}
+
+int geon_camera_tetrad(geon_metric_t m, const double observer[4], double out_tetrad[16]) {
+  if (int rc = check_metric(m)) return rc;
+  if (!observer || !out_tetrad) return fail(GEON_ERR_INVALID, "null buffer");
+  geon_camera cam;
+  std::memset(&cam, 0, sizeof cam);
+  std::memcpy(cam.observer, observer, sizeof cam.observer);
+  cam.fov_y_deg = 60.0;
+  cam.width = cam.height = 1;
+  cam.forward_sign = 1;
+  CameraDesc c;
+  if (int rc = make_camera(m, &cam, 1, c, host_stream())) return rc;
+  std::memcpy(out_tetrad, c.tet, sizeof c.tet);
+  return GEON_OK;
+}
+
+int geon_camera_ray_states(const geon_camera* cam, const double tetrad[16], double du, double dv,
+                           double* out_states) {
+  if (!cam || !tetrad || !out_states || cam->width <= 0 || cam->height <= 0)
+    return fail(GEON_ERR_INVALID, "bad camera arguments");
+  if (cam->forward_sign != 1 && cam->forward_sign != -1) return fail(GEON_ERR_INVALID, "forward_sign must be +1 or -1");
+  CameraDesc c;
+  std::memcpy(c.tet, tetrad, sizeof c.tet);
+  std::memcpy(c.obs, cam->observer, sizeof c.obs);
+  const double fov = cam->fov_y_deg * RADS_PER_DEG;
+  const double aspect = (double)cam->width / (double)cam->height;
+  c.h_img = std::tan(fov * 0.5);
+  c.w_img = c.h_img * aspect;
+  c.width_d = (double)cam->width;
+  c.height_d = (double)cam->height;
+  c.width = cam->width;
+  c.height = cam->height;
+  c.spa = 1;
+  c.inv_spa = 1.0;
+  c.forward_sign = cam->forward_sign;
+  const size_t n = (size_t)(cam->width * cam->height);
+  cudaStream_t s = host_stream();
+  DBuf d;
+  GEON_CUDA(d.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(launch_camera_rays(c, du, dv, d.as<double>(), s));
+  GEON_CUDA(cudaMemcpyAsync(out_states, d.p, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
+                   geon_render_stats* stats, int32_t* pixel_class, int64_t* pixel_steps) {
+  if (int rc = check_metric(m)) return rc;
+  if (!cfg || !rgb) return fail(GEON_ERR_INVALID, "null buffer");
+  if (cfg->precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (cfg->max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
+  cudaStream_t s = host_stream();
+  const int64_t spa = cfg->samples_per_axis < 1 ? 1 : cfg->samples_per_axis;
+  CameraDesc c;
+  if (int rc = make_camera(m, cam, spa, c, s)) return rc;
+  const int64_t npix = cam->width * cam->height;
+  const int64_t nsamp = npix * spa * spa;
+  DBuf dsrgb, dterm, dsteps, dres, drgb, dcls, dpst, ws;
+  GEON_CUDA(dsrgb.alloc(sizeof(float) * 3 * nsamp, s));
+  GEON_CUDA(dterm.alloc(sizeof(int32_t) * nsamp, s));
+  GEON_CUDA(dsteps.alloc(sizeof(int64_t) * nsamp, s));
+  GEON_CUDA(dres.alloc(sizeof(double) * nsamp, s));
+  GEON_CUDA(drgb.alloc(sizeof(float) * 3 * npix, s));
+  GEON_CUDA(dcls.alloc(sizeof(int32_t) * npix, s));
+  GEON_CUDA(dpst.alloc(sizeof(int64_t) * npix, s));
+  const size_t ws_bytes = sizeof(unsigned long long) * 8;
+  GEON_CUDA(ws.alloc(ws_bytes, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, ws_bytes, s));
+  TraceLaunch L = base_launch(m, cfg->step, cfg->max_steps);
+  L.cam = c;
+  L.n = nsamp;
+  L.term = dterm.as<int32_t>();
+  L.steps = dsteps.as<int64_t>();
+  L.resid = dres.as<double>();
+  L.srgb = dsrgb.as<float>();
+  L.show_stars = cfg->show_stars < 0 ? g_show_stars.load() : (cfg->show_stars != 0);
+  for (int q = 0; q < 3; ++q) {
+    L.captured_rgb[q] = cfg->captured_rgb[q];
+    L.diverged_rgb[q] = cfg->diverged_rgb[q];
+  }
+  unsigned long long* wsu = ws.as<unsigned long long>();
+  L.queue = wsu;
+  L.flags = reinterpret_cast<int*>(wsu + 1);
+  unsigned long long* dstats = wsu + 2;  // 6 counters
+  GEON_CUDA(launch_trace_fp64(L, SRC_CAMERA, SINK_RENDER, s));
+  GEON_CUDA(launch_render_reduce(dsrgb.as<float>(), dterm.as<int32_t>(), dsteps.as<int64_t>(),
+                                 dres.as<double>(), npix, spa, drgb.as<float>(), dcls.as<int32_t>(),
+                                 dpst.as<int64_t>(), dstats, s));
+  unsigned long long hst[6];
+  GEON_CUDA(cudaMemcpyAsync(rgb, drgb.p, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, s));
+  if (int rc = copy_out(pixel_class, dcls.p, sizeof(int32_t) * npix, s)) return rc;
+  if (int rc = copy_out(pixel_steps, dpst.p, sizeof(int64_t) * npix, s)) return rc;
+  GEON_CUDA(cudaMemcpyAsync(hst, dstats, sizeof hst, cudaMemcpyDeviceToHost, s));
+  int flags = 0;
+  if (int rc = sync_and_flags(s, L.flags, &flags)) return rc;
+  if (stats) {
+    stats->captured = (int64_t)hst[0];
+    stats->escaped = (int64_t)hst[1];
+    stats->diverged = (int64_t)hst[2];
+    double mr;
+    std::memcpy(&mr, &hst[4], sizeof mr);
+    stats->max_null_residual = mr;
+    stats->avg_steps = (double)(int64_t)hst[3] / (double)npix;
+    stats->total_steps = (int64_t)hst[5];
+  }
+  return singular_status(flags);
+}
+
+int geon_render(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
+                geon_render_stats* stats) {
+  return geon_render_ex(m, cam, cfg, rgb, stats, nullptr, nullptr);
+}
+
+int geon_sky_sample(const double* dir, size_t n, int show_stars, float* rgb) {
+  if (n == 0) return GEON_OK;
+  if (!dir || !rgb) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf dd, dr;
+  GEON_CUDA(dd.alloc(sizeof(double) * 3 * n, s));
+  GEON_CUDA(dr.alloc(sizeof(float) * 3 * n, s));
+  GEON_CUDA(cudaMemcpyAsync(dd.p, dir, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(launch_sky(dd.as<double>(), (int64_t)n, show_stars, dr.as<float>(), s));
+  GEON_CUDA(cudaMemcpyAsync(rgb, dr.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+static int curvature_call(geon_metric_t m, int what, const double* x, size_t n, const double* k, size_t nk,
+                          int k_shared, double* out, int out_width) {
+  if (int rc = check_metric(m)) return rc;
+  if (n == 0) return GEON_OK;
+  if (!x || !out) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf dx, dk, dout, dflags;
+  const size_t kcount = what == 5 ? (k_shared ? nk : nk * n) : 0;
+  GEON_CUDA(dx.alloc(sizeof(double) * 4 * n, s));
+  GEON_CUDA(dk.alloc(sizeof(double) * 4 * kcount, s));
+  GEON_CUDA(dout.alloc(sizeof(double) * n * out_width, s));
+  GEON_CUDA(dflags.alloc(sizeof(int), s));
+  GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
+  GEON_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, s));
+  if (kcount) GEON_CUDA(cudaMemcpyAsync(dk.p, k, sizeof(double) * 4 * kcount, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(launch_curvature(m->desc, what, dx.as<double>(), (int64_t)n, dk.as<double>(), (int64_t)nk,
+                             k_shared, dout.as<double>(), dflags.as<int>(), s));
+  GEON_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double) * n * out_width, cudaMemcpyDeviceToHost, s));
+  int flags = 0;
+  if (int rc = sync_and_flags(s, dflags.as<int>(), &flags)) return rc;
+  return singular_status(flags);
+}
+
+int geon_riemann(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 0, x, n, nullptr, 0, 1, out, 256); }
+int geon_ricci(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 1, x, n, nullptr, 0, 1, out, 16); }
+int geon_ricci_scalar(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 2, x, n, nullptr, 0, 1, out, 1); }
+int geon_einstein(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 3, x, n, nullptr, 0, 1, out, 16); }
+int geon_stress_energy(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 4, x, n, nullptr, 0, 1, out, 16); }
+
+int geon_nec_contraction(geon_metric_t m, const double* x, size_t n, const double* k, size_t nk, int k_shared,
+                         double* out) {
+  if (nk == 0 || n == 0) return GEON_OK;
+  if (!k) return fail(GEON_ERR_INVALID, "null k");
+  return curvature_call(m, 5, x, n, k, nk, k_shared, out, (int)nk);
+}
+
+int geon_wec_contraction(geon_metric_t m, const double* x, size_t n, const double* u, size_t nu, int u_shared,
+                         double* out) {
+  return geon_nec_contraction(m, x, n, u, nu, u_shared, out);
+}
+
+int geon_equatorial_rays(geon_metric_t m, double r_obs, const double* alpha, size_t n, double* out_states) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "equatorial rays need a Schwarzschild metric");
+  if (n == 0) return GEON_OK;
+  if (!alpha || !out_states) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf da, dout;
+  GEON_CUDA(da.alloc(sizeof(double) * n, s));
+  GEON_CUDA(dout.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(cudaMemcpyAsync(da.p, alpha, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(launch_equatorial_rays(m->desc.p[0], r_obs, da.as<double>(), (int64_t)n, dout.as<double>(), s));
+  GEON_CUDA(cudaMemcpyAsync(out_states, dout.p, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+// Classify rays launched at the given angles on stream s (device buffers).
+static int classify_dev(geon_metric_t m, double r_obs, const double* d_alpha, int64_t n, double step,
+                        int64_t max_steps, int32_t* d_term, int64_t* d_steps, cudaStream_t s) {
+  DBuf ws;
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 2, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 2, s));
+  TraceLaunch L = base_launch(m, step, max_steps);
+  L.n = n;
+  L.alpha = d_alpha;
+  L.r_obs = r_obs;
+  L.term = d_term;
+  L.steps = d_steps;
+  L.queue = ws.as<unsigned long long>();
+  L.flags = reinterpret_cast<int*>(L.queue + 1);
+  GEON_CUDA(launch_trace_fp64(L, SRC_EQUATORIAL, SINK_SHADOW, s));
+  return GEON_OK;
+}
+
+int geon_shadow_classify(geon_metric_t m, double r_obs, const double* alpha, size_t n, double step,
+                         int64_t max_steps, int precision, int32_t* term, int64_t* steps) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow classification needs a Schwarzschild metric");
+  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (n == 0) return GEON_OK;
+  if (!alpha || !term) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf da, dt, dst;
+  GEON_CUDA(da.alloc(sizeof(double) * n, s));
+  GEON_CUDA(dt.alloc(sizeof(int32_t) * n, s));
+  GEON_CUDA(dst.alloc(sizeof(int64_t) * n, s));
+  GEON_CUDA(cudaMemcpyAsync(da.p, alpha, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (int rc = classify_dev(m, r_obs, da.as<double>(), (int64_t)n, step, max_steps, dt.as<int32_t>(),
+                            dst.as<int64_t>(), s))
+    return rc;
+  GEON_CUDA(cudaMemcpyAsync(term, dt.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  if (int rc = copy_out(steps, dst.p, sizeof(int64_t) * n, s)) return rc;
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+// Bisection of bin/validate_shadow.rs:70-79, evaluated L levels at a time: for
+// each bracket every midpoint the next L sequential halvings could visit (a
+// complete binary tree of 2^L - 1 launch angles, built with the same
+// 0.5*(lo+hi) arithmetic) is traced in one launch, then the sequential path is
+// replayed through the tree. The result equals the sequential loop bit for
+// bit, with ceil(iters / L) dependent launches instead of iters.
+int geon_shadow_bisect(geon_metric_t m, double r_obs, const double* lo, const double* hi, size_t nb, int iters,
+                       double step, int64_t max_steps, int precision, double* alpha_c, double* lo_out,
+                       double* hi_out, int64_t* steps_out) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow bisection needs a Schwarzschild metric");
+  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (nb == 0) return GEON_OK;
+  if (!lo || !hi || !alpha_c || iters < 0) return fail(GEON_ERR_INVALID, "bad bisection arguments");
+  std::vector<double> vlo(lo, lo + nb), vhi(hi, hi + nb);
+  std::vector<int64_t> vsteps(nb, 0);
+  const int64_t target_rays = 16384;
+  int Lmax = 1;
+  while (Lmax < 16 && (int64_t)nb * ((1LL << (Lmax + 1)) - 1) <= target_rays) ++Lmax;
+  cudaStream_t s = host_stream();
+  int remaining = iters;
+  const int64_t cap = (int64_t)nb * ((1LL << Lmax) - 1);
+  DBuf da, dt, dst;
+  GEON_CUDA(da.alloc(sizeof(double) * cap, s));
+  GEON_CUDA(dt.alloc(sizeof(int32_t) * cap, s));
+  GEON_CUDA(dst.alloc(sizeof(int64_t) * cap, s));
+  std::vector<double> alpha(cap), node_lo(cap), node_hi(cap);
+  std::vector<int32_t> term(cap);
+  std::vector<int64_t> st(cap);
+  while (remaining > 0) {
+    const int L = remaining < Lmax ? remaining : Lmax;
+    const int64_t per = (1LL << L) - 1;
+    // heap-ordered tree per bracket: node 1 is the root, children 2i / 2i+1
+    for (size_t b = 0; b < nb; ++b) {
+      double* a = &alpha[b * per];
+      double* nl = &node_lo[b * per];
+      double* nh = &node_hi[b * per];
+      nl[0] = vlo[b];
+      nh[0] = vhi[b];
+      for (int64_t i = 1; i <= per; ++i) {
+        const double l = nl[i - 1], h = nh[i - 1];
+        const double mid = 0.5 * (l + h);
+        a[i - 1] = mid;
+        if (2 * i <= per) {  // left child: not captured -> hi = mid
+          nl[2 * i - 1] = l;
+          nh[2 * i - 1] = mid;
+        }
+        if (2 * i + 1 <= per) {  // right child: captured -> lo = mid
+          nl[2 * i] = mid;
+          nh[2 * i] = h;
+        }
+      }
+    }
+    const int64_t nr = (int64_t)nb * per;
+    GEON_CUDA(cudaMemcpyAsync(da.p, alpha.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, s));
+    if (int rc = classify_dev(m, r_obs, da.as<double>(), nr, step, max_steps, dt.as<int32_t>(),
+                              dst.as<int64_t>(), s))
+      return rc;
+    GEON_CUDA(cudaMemcpyAsync(term.data(), dt.p, sizeof(int32_t) * nr, cudaMemcpyDeviceToHost, s));
+    GEON_CUDA(cudaMemcpyAsync(st.data(), dst.p, sizeof(int64_t) * nr, cudaMemcpyDeviceToHost, s));
+    GEON_CUDA(cudaStreamSynchronize(s));
+    for (size_t b = 0; b < nb; ++b) {
+      int64_t node = 1;
+      for (int d = 0; d < L; ++d) {
+        const double mid = alpha[b * per + node - 1];
+        vsteps[b] += st[b * per + node - 1];
+        if (term[b * per + node - 1] == TERM_CAPTURED) {
+          vlo[b] = mid;
+          node = 2 * node + 1;
+        } else {
+          vhi[b] = mid;
+          node = 2 * node;
+        }
+      }
+    }
+    remaining -= L;
+  }
+  for (size_t b = 0; b < nb; ++b) {
+    alpha_c[b] = 0.5 * (vlo[b] + vhi[b]);
+    if (lo_out) lo_out[b] = vlo[b];
+    if (hi_out) hi_out[b] = vhi[b];
+    if (steps_out) steps_out[b] = vsteps[b];
+  }
+  return GEON_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+// Internal types shared by the CUDA translation units and the C ABI layer.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/geon_gpu.h"
+
+namespace geon {
+
+enum : int { TERM_NONE = -1, TERM_DIVERGED = 0, TERM_CAPTURED = 1, TERM_ESCAPED = 2 };
+enum : int { KIND_MINKOWSKI = 0, KIND_SCHWARZSCHILD = 1, KIND_ALCUBIERRE = 2, KIND_MORRIS_THORNE = 3 };
+
+// Per-metric constants, passed by value to every kernel (kernel parameters live
+// in the constant bank, so every lane reads them through the constant cache).
+struct MetricDesc {
+  int kind;
+  double p[4];       // the reference struct's fields, in declaration order
+  double capture_r;  // Schwarzschild: horizon_pad * 2.0 * mass   (schwarzschild.rs:114)
+  double escape_r;   // Schwarzschild: escape_radius * mass        (schwarzschild.rs:116)
+  double alc_denom;  // Alcubierre: 2.0 * tanh(R / s)               (alcubierre.rs:42)
+};
+
+// Camera for device-side ray generation (camera.rs:113-160 with the values that
+// the reference recomputes per pixel hoisted: they are identical every time).
+struct CameraDesc {
+  double tet[4][4];  // rows e_a^mu
+  double obs[4];
+  double h_img;      // tan(fov_y_rad * 0.5), from the host libm as in the reference
+  double w_img;      // h_img * aspect
+  double width_d, height_d;
+  int64_t width, height;
+  int64_t spa;       // samples per axis
+  double inv_spa;
+  int forward_sign;
+};
+
+// Sources of initial states.
+enum : int { SRC_ARRAY = 0, SRC_CAMERA = 1, SRC_EQUATORIAL = 2 };
+// Where results go.
+enum : int { SINK_TRACE = 0, SINK_RENDER = 1, SINK_SHADOW = 2 };
+
+struct TraceLaunch {
+  MetricDesc M;
+  CameraDesc cam;
+  int64_t n;           // rays in the job
+  double step;
+  double half_step;    // 0.5 * step   (integrator.rs:24: `0.5 * h * k`, left-associated)
+  double sixth;        // step / 6.0   (integrator.rs:36)
+  int64_t max_steps;
+  // SRC_ARRAY
+  const double* y0;    // n x 8 (AoS, the reference's State layout)
+  // SRC_EQUATORIAL (bin/validate_shadow.rs:20-35)
+  const double* alpha; // n launch angles
+  double r_obs;
+  // SINK_TRACE
+  int32_t* term;
+  double* yfinal;      // n x 8
+  int64_t* steps;
+  double* resid;
+  // SINK_RENDER: per-sample results, reduced per pixel afterwards
+  float* srgb;         // n x 3
+  int show_stars;
+  float captured_rgb[3];  // RenderConfig::captured_rgb (render.rs:20)
+  float diverged_rgb[3];  // RenderConfig::diverged_rgb (render.rs:25)
+  // work queue
+  unsigned long long* queue;  // next unclaimed ray index
+  int* flags;                 // bit 0: a metric became singular (inverse of g failed)
+};
+
+// ---- launchers (trace_fp64.cu) ----
+cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStream_t s);
+cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,
+                                 const double* resid, int64_t npix, int64_t spa, float* rgb,
+                                 int32_t* pclass, int64_t* psteps, unsigned long long* stats,
+                                 cudaStream_t s);
+cudaError_t launch_pointwise(const MetricDesc& M, int what, const double* in, int64_t n, double* out,
+                             int32_t* iout, int* flags, cudaStream_t s);
+cudaError_t launch_tetrad(const MetricDesc& M, const double* obs, double* out16, int* status,
+                          cudaStream_t s);
+cudaError_t launch_metric_init(MetricDesc* d_desc, cudaStream_t s);
+cudaError_t launch_sky(const double* dir, int64_t n, int show, float* rgb, cudaStream_t s);
+int trace_fp64_blocks_per_sm(int kind, int src, int sink);
+
+// ---- launchers (curvature_fp64.cu) ----
+// what: 0 riemann, 1 ricci, 2 ricci_scalar, 3 einstein, 4 stress_energy, 5 nec
+cudaError_t launch_curvature(const MetricDesc& M, int what, const double* x, int64_t n,
+                             const double* k, int64_t nk, int k_shared, double* out, int* flags,
+                             cudaStream_t s);
+
+// pointwise "what" codes
+enum : int { PW_G = 0, PW_DG = 1, PW_GINV = 2, PW_CHRISTOFFEL = 3, PW_TERMINATE = 4, PW_ASYM = 5 };
+
+}  // namespace geon

@@ -1,0 +1,406 @@
+// FP64 device functors for the four metrics: g, g^-1, Christoffel symbols, the
+// geodesic right-hand side, termination and the escape direction.
+//
+// Parity contract: with --fmad=false and the deterministic sin/cos/tanh of
+// devmath.cuh, every function here returns the bits the reference's Rust code
+// returns for the same inputs (the CPU oracle in oracle/ checks this). Rules
+// that keep it so:
+//  * operations appear in the reference's order, sums left-associated;
+//  * a term of an accumulation that starts at +0.0 (all of the reference's sums
+//    do) may be skipped when it is exactly zero: x + (+-0) == x for x != 0, and
+//    such a sum can never become -0, so the sign of a skipped zero is
+//    irrelevant. The sparse functors below use only this and exact identities
+//    (x * 1.0 == x, -(a/b) == (-a)/b, 2.0 * x exact).
+#pragma once
+#include "devmath.cuh"
+#include "internal.h"
+
+namespace geon {
+
+constexpr double FD_H = 1e-5;  // Metric::fd_step default (metric/mod.rs:73-75)
+
+// types.rs:22-30
+__device__ __forceinline__ double dot4(const double g[16], const double a[4], const double b[4]) {
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s += g[4 * i + j] * a[i] * b[j];
+  return s;
+}
+
+// Stand-in for nalgebra's Matrix4::try_inverse (types.rs:34-47): adjugate by 2x2
+// minors (Laplace expansion; D. Eberly, Geometric Tools 2008). The CPU oracle
+// uses the identical sequence. Returns false when det == 0.
+__device__ __forceinline__ bool inv4(const double a[16], double out[16]) {
+  const double a00 = a[0], a01 = a[1], a02 = a[2], a03 = a[3];
+  const double a10 = a[4], a11 = a[5], a12 = a[6], a13 = a[7];
+  const double a20 = a[8], a21 = a[9], a22 = a[10], a23 = a[11];
+  const double a30 = a[12], a31 = a[13], a32 = a[14], a33 = a[15];
+  const double s0 = a00 * a11 - a10 * a01;
+  const double s1 = a00 * a12 - a10 * a02;
+  const double s2 = a00 * a13 - a10 * a03;
+  const double s3 = a01 * a12 - a11 * a02;
+  const double s4 = a01 * a13 - a11 * a03;
+  const double s5 = a02 * a13 - a12 * a03;
+  const double c5 = a22 * a33 - a32 * a23;
+  const double c4 = a21 * a33 - a31 * a23;
+  const double c3 = a21 * a32 - a31 * a22;
+  const double c2 = a20 * a33 - a30 * a23;
+  const double c1 = a20 * a32 - a30 * a22;
+  const double c0 = a20 * a31 - a30 * a21;
+  const double det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+  const bool ok = det != 0.0;
+  const double id = 1.0 / det;
+  out[0] = (a11 * c5 - a12 * c4 + a13 * c3) * id;
+  out[1] = (-a01 * c5 + a02 * c4 - a03 * c3) * id;
+  out[2] = (a31 * s5 - a32 * s4 + a33 * s3) * id;
+  out[3] = (-a21 * s5 + a22 * s4 - a23 * s3) * id;
+  out[4] = (-a10 * c5 + a12 * c2 - a13 * c1) * id;
+  out[5] = (a00 * c5 - a02 * c2 + a03 * c1) * id;
+  out[6] = (-a30 * s5 + a32 * s2 - a33 * s1) * id;
+  out[7] = (a20 * s5 - a22 * s2 + a23 * s1) * id;
+  out[8] = (a10 * c4 - a11 * c2 + a13 * c0) * id;
+  out[9] = (-a00 * c4 + a01 * c2 - a03 * c0) * id;
+  out[10] = (a30 * s4 - a31 * s2 + a33 * s0) * id;
+  out[11] = (-a20 * s4 + a21 * s2 - a23 * s0) * id;
+  out[12] = (-a10 * c3 + a11 * c1 - a12 * c0) * id;
+  out[13] = (a00 * c3 - a01 * c1 + a02 * c0) * id;
+  out[14] = (-a30 * s3 + a31 * s1 - a32 * s0) * id;
+  out[15] = (a20 * s3 - a21 * s1 + a22 * s0) * id;
+  if (!ok) {
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) out[i] = nan;
+  }
+  return ok;
+}
+
+// ---------------------------------------------------------------------------
+// g(x) for each metric (dense 4x4, row-major)
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void metric_g(const MetricDesc& M, const double x[4], double g[16]) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) g[i] = 0.0;
+  if (K == KIND_MINKOWSKI) {  // minkowski.rs:11-18
+    g[0] = -1.0; g[5] = 1.0; g[10] = 1.0; g[15] = 1.0;
+  } else if (K == KIND_SCHWARZSCHILD) {  // schwarzschild.rs:33-45
+    const double r = x[1], theta = x[2], m = M.p[0];
+    const double f = 1.0 - 2.0 * m / r;
+    double sin_t, cos_t;
+    dm::sincos_det(theta, &sin_t, &cos_t);
+    g[0] = -f;
+    g[5] = 1.0 / f;
+    g[10] = r * r;
+    g[15] = r * r * sin_t * sin_t;
+  } else if (K == KIND_ALCUBIERRE) {  // alcubierre.rs:33-63
+    const double R = M.p[0], s = M.p[1], v = M.p[2], ship_x = M.p[3];
+    const double dx = x[1] - ship_x, dy = x[2], dz = x[3];
+    const double r_s = sqrt(dx * dx + dy * dy + dz * dz);
+    const double t_plus = dm::tanh_det((r_s + R) / s);
+    const double t_minus = dm::tanh_det((r_s - R) / s);
+    const double f = (t_plus - t_minus) / M.alc_denom;
+    g[0] = -1.0 + v * v * f * f;
+    g[1] = -v * f;
+    g[4] = -v * f;
+    g[5] = 1.0;
+    g[10] = 1.0;
+    g[15] = 1.0;
+  } else {  // morris_thorne.rs:22-36
+    const double l = x[1], theta = x[2], b0 = M.p[0];
+    const double r2 = b0 * b0 + l * l;
+    double sin_t, cos_t;
+    dm::sincos_det(theta, &sin_t, &cos_t);
+    g[0] = -1.0;
+    g[5] = 1.0;
+    g[10] = r2;
+    g[15] = r2 * sin_t * sin_t;
+  }
+}
+
+// g^-1: overrides for Minkowski and Schwarzschild, inv4(g) otherwise (mod.rs:46-48).
+template <int K>
+__device__ __forceinline__ bool metric_g_inv(const MetricDesc& M, const double x[4], double gi[16]) {
+  if (K == KIND_MINKOWSKI) {
+    metric_g<K>(M, x, gi);
+    return true;
+  } else if (K == KIND_SCHWARZSCHILD) {  // schwarzschild.rs:47-59
+#pragma unroll
+    for (int i = 0; i < 16; ++i) gi[i] = 0.0;
+    const double r = x[1], theta = x[2], m = M.p[0];
+    const double f = 1.0 - 2.0 * m / r;
+    double sin_t, cos_t;
+    dm::sincos_det(theta, &sin_t, &cos_t);
+    gi[0] = -1.0 / f;
+    gi[5] = f;
+    gi[10] = 1.0 / (r * r);
+    gi[15] = 1.0 / (r * r * sin_t * sin_t);
+    return true;
+  } else {
+    double g[16];
+    metric_g<K>(M, x, g);
+    return inv4(g, gi);
+  }
+}
+
+// Default dg: central differences with (gp - gm) / two_h (mod.rs:25-43).
+template <int K>
+__device__ __forceinline__ void metric_dg_fd(const MetricDesc& M, const double x[4], double dg[64]) {
+#pragma unroll 1
+  for (int alpha = 0; alpha < 4; ++alpha) {
+    double xp[4] = {x[0], x[1], x[2], x[3]};
+    double xm[4] = {x[0], x[1], x[2], x[3]};
+    xp[alpha] += FD_H;
+    xm[alpha] -= FD_H;
+    double gp[16], gm[16];
+    metric_g<K>(M, xp, gp);
+    metric_g<K>(M, xm, gm);
+    const double two_h = 2.0 * FD_H;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) dg[16 * alpha + i] = (gp[i] - gm[i]) / two_h;
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void metric_dg(const MetricDesc& M, const double x[4], double dg[64]) {
+  if (K == KIND_MINKOWSKI) {
+#pragma unroll
+    for (int i = 0; i < 64; ++i) dg[i] = 0.0;
+  } else {
+    metric_dg_fd<K>(M, x, dg);
+  }
+}
+
+// Schwarzschild analytic Christoffel symbols (schwarzschild.rs:61-107).
+__device__ __forceinline__ void christoffel_schw(const MetricDesc& M, const double x[4], double G[64]) {
+#pragma unroll
+  for (int i = 0; i < 64; ++i) G[i] = 0.0;
+  const double r = x[1], theta = x[2], m = M.p[0];
+  const double f = 1.0 - 2.0 * m / r;
+  double sin_t, cos_t;
+  dm::sincos_det(theta, &sin_t, &cos_t);
+  const double gtr = m / (r * r * f);
+  G[0 * 16 + 0 * 4 + 1] = gtr;
+  G[0 * 16 + 1 * 4 + 0] = gtr;
+  G[1 * 16 + 0 * 4 + 0] = m * f / (r * r);
+  G[1 * 16 + 1 * 4 + 1] = -m / (r * r * f);
+  G[1 * 16 + 2 * 4 + 2] = -(r - 2.0 * m);
+  G[1 * 16 + 3 * 4 + 3] = -(r - 2.0 * m) * sin_t * sin_t;
+  const double gtheta_rt = 1.0 / r;
+  G[2 * 16 + 1 * 4 + 2] = gtheta_rt;
+  G[2 * 16 + 2 * 4 + 1] = gtheta_rt;
+  G[2 * 16 + 3 * 4 + 3] = -sin_t * cos_t;
+  G[3 * 16 + 1 * 4 + 3] = 1.0 / r;
+  G[3 * 16 + 3 * 4 + 1] = 1.0 / r;
+  const double cot = fabs(sin_t) < 1e-8 ? 0.0 : cos_t / sin_t;
+  G[3 * 16 + 2 * 4 + 3] = cot;
+  G[3 * 16 + 3 * 4 + 2] = cot;
+}
+
+// Generic Christoffel symbols from g^-1 and the FD dg (mod.rs:51-69), dense.
+template <int K>
+__device__ __forceinline__ bool christoffel_generic(const MetricDesc& M, const double x[4], double G[64]) {
+  double ginv[16];
+  const bool ok = metric_g_inv<K>(M, x, ginv);
+  double dg[64];
+  metric_dg<K>(M, x, dg);
+#pragma unroll 1
+  for (int mu = 0; mu < 4; ++mu)
+#pragma unroll
+    for (int alpha = 0; alpha < 4; ++alpha)
+#pragma unroll
+      for (int beta = 0; beta < 4; ++beta) {
+        double s = 0.0;
+#pragma unroll
+        for (int sigma = 0; sigma < 4; ++sigma)
+          s += ginv[4 * mu + sigma] *
+               (dg[16 * alpha + 4 * sigma + beta] + dg[16 * beta + 4 * sigma + alpha] -
+                dg[16 * sigma + 4 * alpha + beta]);
+        G[16 * mu + 4 * alpha + beta] = 0.5 * s;
+      }
+  return ok;
+}
+
+template <int K>
+__device__ __forceinline__ bool metric_christoffel(const MetricDesc& M, const double x[4], double G[64]) {
+  if (K == KIND_MINKOWSKI) {
+#pragma unroll
+    for (int i = 0; i < 64; ++i) G[i] = 0.0;
+    return true;
+  } else if (K == KIND_SCHWARZSCHILD) {
+    christoffel_schw(M, x, G);
+    return true;
+  } else {
+    return christoffel_generic<K>(M, x, G);
+  }
+}
+
+// Termination tests (minkowski.rs:32-39, schwarzschild.rs:109-121, alcubierre.rs:65-75,
+// morris_thorne.rs:38-48).
+template <int K>
+__device__ __forceinline__ int metric_terminate(const MetricDesc& M, const double x[4]) {
+  if (K == KIND_MINKOWSKI) {
+    const double r2 = x[1] * x[1] + x[2] * x[2] + x[3] * x[3];
+    return r2 > 1e6 ? TERM_ESCAPED : TERM_NONE;
+  } else if (K == KIND_SCHWARZSCHILD) {
+    const double r = x[1];
+    if (!isfinite(r)) return TERM_DIVERGED;
+    if (r < M.capture_r) return TERM_CAPTURED;
+    if (r > M.escape_r) return TERM_ESCAPED;
+    return TERM_NONE;
+  } else if (K == KIND_ALCUBIERRE) {
+    const double r2 = x[1] * x[1] + x[2] * x[2] + x[3] * x[3];
+    if (!isfinite(r2)) return TERM_DIVERGED;
+    return r2 > 1e6 ? TERM_ESCAPED : TERM_NONE;
+  } else {
+    const double l = x[1];
+    if (!isfinite(l)) return TERM_DIVERGED;
+    return fabs(l) > 1000.0 ? TERM_ESCAPED : TERM_NONE;
+  }
+}
+
+// Escape direction (mod.rs:91-108 default; alcubierre.rs:81-88; morris_thorne.rs:54-77).
+template <int K>
+__device__ __forceinline__ void metric_asymptotic_direction(const double x[4], const double p[4],
+                                                            double out[3]) {
+  if (K == KIND_ALCUBIERRE) {
+    const double vx = p[1], vy = p[2], vz = p[3];
+    const double n = fmax(sqrt(vx * vx + vy * vy + vz * vz), 1e-30);
+    out[0] = vx / n; out[1] = vy / n; out[2] = vz / n;
+    return;
+  }
+  double sin_t, cos_t, sin_p, cos_p;
+  dm::sincos_det(x[2], &sin_t, &cos_t);
+  dm::sincos_det(x[3], &sin_p, &cos_p);
+  const double pr = p[1], pt = p[2], pp = p[3];
+  if (K == KIND_MORRIS_THORNE) {
+    const double l = x[1];
+    const double r_eff = fmax(fabs(l), 1e-30);
+    const double vx = sin_t * cos_p * pr + r_eff * cos_t * cos_p * pt - r_eff * sin_t * sin_p * pp;
+    const double vy = sin_t * sin_p * pr + r_eff * cos_t * sin_p * pt + r_eff * sin_t * cos_p * pp;
+    const double vz = cos_t * pr - r_eff * sin_t * pt;
+    const double n = fmax(sqrt(vx * vx + vy * vy + vz * vz), 1e-30);
+    const double sign = l < 0.0 ? -1.0 : 1.0;
+    out[0] = sign * vx / n; out[1] = vy / n; out[2] = vz / n;
+  } else {
+    const double r = x[1];
+    const double vx = sin_t * cos_p * pr + r * cos_t * cos_p * pt - r * sin_t * sin_p * pp;
+    const double vy = sin_t * sin_p * pr + r * cos_t * sin_p * pt + r * sin_t * cos_p * pp;
+    const double vz = cos_t * pr - r * sin_t * pt;
+    const double n = fmax(sqrt(vx * vx + vy * vy + vz * vz), 1e-30);
+    out[0] = vx / n; out[1] = vy / n; out[2] = vz / n;
+  }
+}
+
+// x + 0.0 (the first addition of a sum that starts at +0.0) without spending an
+// FP64 instruction: only -0.0 changes (to +0.0).
+__device__ __forceinline__ double plus_zero(double x) {
+  const long long b = __double_as_longlong(x);
+  return b == (long long)0x8000000000000000ULL ? 0.0 : x;
+}
+
+// ---------------------------------------------------------------------------
+// Geodesic right-hand side (geodesic.rs:38-59): k = (p, -Gamma^mu_ab p^a p^b).
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ bool geodesic_rhs(const MetricDesc& M, const double y[8], double k[8]) {
+  k[0] = y[4]; k[1] = y[5]; k[2] = y[6]; k[3] = y[7];
+  const double p0 = y[4], p1 = y[5], p2 = y[6], p3 = y[7];
+  if (K == KIND_MINKOWSKI) {
+    // Every term is 0 * p * p: the sum is +0.0 and the derivative -0.0.
+    k[4] = -0.0; k[5] = -0.0; k[6] = -0.0; k[7] = -0.0;
+    return true;
+  } else if (K == KIND_SCHWARZSCHILD) {
+    // schwarzschild.rs:61-107 fused with the sum; only the nonzero entries
+    // contribute (alpha-major, beta-minor order kept).
+    const double r = y[1], theta = y[2], m = M.p[0];
+    const double f = 1.0 - 2.0 * m / r;
+    double sin_t, cos_t;
+    dm::sincos_det(theta, &sin_t, &cos_t);
+    const double rr = r * r;
+    const double rrf = rr * f;
+    const double gtr = m / rrf;            // Gamma^t_tr = Gamma^t_rt
+    const double g_r_tt = m * f / rr;      // Gamma^r_tt
+    const double g_r_rr = -gtr;            // -m/(r r f) == -(m/(r r f))
+    const double r2m = r - 2.0 * m;
+    const double g_r_thth = -r2m;          // Gamma^r_thth
+    const double g_r_phph = -r2m * sin_t * sin_t;
+    const double ir = 1.0 / r;             // Gamma^th_rth, Gamma^ph_rph
+    const double g_th_phph = -sin_t * cos_t;
+    const double cot = fabs(sin_t) < 1e-8 ? 0.0 : cos_t / sin_t;
+    double s;
+    s = plus_zero(gtr * p0 * p1);
+    s += gtr * p1 * p0;
+    k[4] = -s;
+    s = plus_zero(g_r_tt * p0 * p0);
+    s += g_r_rr * p1 * p1;
+    s += g_r_thth * p2 * p2;
+    s += g_r_phph * p3 * p3;
+    k[5] = -s;
+    s = plus_zero(ir * p1 * p2);
+    s += ir * p2 * p1;
+    s += g_th_phph * p3 * p3;
+    k[6] = -s;
+    s = plus_zero(ir * p1 * p3);
+    s += cot * p2 * p3;
+    s += ir * p3 * p1;
+    s += cot * p3 * p2;
+    k[7] = -s;
+    return true;
+  } else {
+    double G[64];
+    const bool ok = christoffel_generic<K>(M, y, G);
+#pragma unroll
+    for (int mu = 0; mu < 4; ++mu) {
+      double s = 0.0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) s += G[16 * mu + 4 * a + b] * y[4 + a] * y[4 + b];
+      k[4 + mu] = -s;
+    }
+    return ok;
+  }
+}
+
+// Classical RK4 (integrator.rs:16-40) with the reference's grouping:
+// y + (0.5*h)*k, y + h*k3, and y + (h/6)*(((k1 + 2 k2) + 2 k3) + k4).
+template <int K>
+__device__ __forceinline__ bool rk4_step(const MetricDesc& M, const double y[8], double h,
+                                         double half_h, double sixth, double out[8]) {
+  double k[8], acc[8], ys[8];
+  bool ok = geodesic_rhs<K>(M, y, k);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    acc[i] = k[i];
+    ys[i] = y[i] + half_h * k[i];
+  }
+  ok &= geodesic_rhs<K>(M, ys, k);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    acc[i] = acc[i] + 2.0 * k[i];
+    ys[i] = y[i] + half_h * k[i];
+  }
+  ok &= geodesic_rhs<K>(M, ys, k);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    acc[i] = acc[i] + 2.0 * k[i];
+    ys[i] = y[i] + h * k[i];
+  }
+  ok &= geodesic_rhs<K>(M, ys, k);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out[i] = y[i] + sixth * (acc[i] + k[i]);
+  return ok;
+}
+
+// Residual |g(p, p)| at the position of y (geodesic.rs:82-84), dense dot4.
+template <int K>
+__device__ __forceinline__ double null_residual(const MetricDesc& M, const double y[8]) {
+  double g[16];
+  metric_g<K>(M, y, g);
+  const double p[4] = {y[4], y[5], y[6], y[7]};
+  return fabs(dot4(g, p, p));
+}
+
+}  // namespace geon

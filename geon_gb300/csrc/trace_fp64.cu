@@ -1,0 +1,480 @@
+// FP64 parity path: persistent ray-tracing kernel and its helpers.
+//
+// One thread owns one ray at a time; the ray state (8 doubles) stays in
+// registers for its whole life. Each warp pulls ray indices from a device work
+// queue with one atomic per refill (ballot + popc + shuffle), so a lane whose
+// ray is captured or escapes picks up a fresh ray at the next step instead of
+// idling until the slowest ray of its warp finishes.
+//
+// Compiled with --fmad=false: every FP64 result must match the CPU oracle.
+#include <cuda_runtime.h>
+
+#include "internal.h"
+#include "metric_fp64.cuh"
+#include "sky.cuh"
+
+namespace geon {
+
+// ---------------------------------------------------------------------------
+// Sources of initial states
+// ---------------------------------------------------------------------------
+// camera.rs:113-160 (ray_state_sub), with forward_sign = +1 the reference.
+__device__ __forceinline__ void camera_ray(const CameraDesc& c, int64_t ray, double y[8]) {
+  const int64_t spa2 = c.spa * c.spa;
+  const int64_t pix = ray / spa2;
+  const int64_t sub = ray - pix * spa2;
+  const int64_t sj = sub / c.spa, si = sub - sj * c.spa;
+  const int64_t j = pix / c.width, i = pix - j * c.width;
+  const double du = ((double)si + 0.5) * c.inv_spa;
+  const double dv = ((double)sj + 0.5) * c.inv_spa;
+  const double u = (2.0 * ((double)i + du) / c.width_d - 1.0) * c.w_img;
+  const double v = -(2.0 * ((double)j + dv) / c.height_d - 1.0) * c.h_img;
+  const double fs = (double)c.forward_sign;
+  const double dx = -fs;
+  const double dy = -v;
+  const double dz = c.forward_sign == 1 ? u : fs * u;
+  const double norm = sqrt(dx * dx + dy * dy + dz * dz);
+  const double n1 = dx / norm, n2 = dy / norm, n3 = dz / norm;
+#pragma unroll
+  for (int mu = 0; mu < 4; ++mu) y[mu] = c.obs[mu];
+#pragma unroll
+  for (int mu = 0; mu < 4; ++mu)
+    y[4 + mu] = c.tet[0][mu] + n1 * c.tet[1][mu] + n2 * c.tet[2][mu] + n3 * c.tet[3][mu];
+}
+
+// bin/validate_shadow.rs:20-35
+__device__ __forceinline__ void equatorial_ray(double m, double r_obs, double alpha, double y[8]) {
+  const double f = 1.0 - 2.0 * m / r_obs;
+  double sin_a, cos_a;
+  dm::sincos_det(alpha, &sin_a, &cos_a);
+  const double sf = sqrt(f);
+  y[0] = 0.0;
+  y[1] = r_obs;
+  y[2] = 1.5707963267948966;  // FRAC_PI_2
+  y[3] = 0.0;
+  y[4] = 1.0 / sf;
+  y[5] = -cos_a * sf;
+  y[6] = 0.0;
+  y[7] = sin_a / r_obs;
+}
+
+template <int SRC>
+__device__ __forceinline__ void load_ray(const TraceLaunch& L, int64_t ray, double y[8]) {
+  if (SRC == SRC_ARRAY) {
+    const double2* p = reinterpret_cast<const double2*>(L.y0 + 8 * ray);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double2 v = p[q];
+      y[2 * q] = v.x;
+      y[2 * q + 1] = v.y;
+    }
+  } else if (SRC == SRC_CAMERA) {
+    camera_ray(L.cam, ray, y);
+  } else {
+    equatorial_ray(L.M.p[0], L.r_obs, L.alpha[ray], y);
+  }
+}
+
+template <int K, int SINK>
+__device__ __forceinline__ void store_ray(const TraceLaunch& L, int64_t ray, int term,
+                                          const double y[8], int64_t steps) {
+  if (SINK == SINK_SHADOW) {
+    L.term[ray] = term;
+    if (L.steps) L.steps[ray] = steps;
+    return;
+  }
+  const double resid = null_residual<K>(L.M, y);
+  if (SINK == SINK_TRACE) {
+    L.term[ray] = term;
+    double2* o = reinterpret_cast<double2*>(L.yfinal + 8 * ray);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_double2(y[2 * q], y[2 * q + 1]);
+    L.steps[ray] = steps;
+    L.resid[ray] = resid;
+  } else {  // SINK_RENDER (render.rs:77-101)
+    float rgb[3];
+    if (term == TERM_CAPTURED) {
+      rgb[0] = L.captured_rgb[0]; rgb[1] = L.captured_rgb[1]; rgb[2] = L.captured_rgb[2];
+    } else if (term == TERM_DIVERGED) {
+      rgb[0] = L.diverged_rgb[0]; rgb[1] = L.diverged_rgb[1]; rgb[2] = L.diverged_rgb[2];
+    } else {
+      double dir[3];
+      metric_asymptotic_direction<K>(y, y + 4, dir);
+      sky_sample(dir, L.show_stars != 0, rgb);
+    }
+    L.srgb[3 * ray + 0] = rgb[0];
+    L.srgb[3 * ray + 1] = rgb[1];
+    L.srgb[3 * ray + 2] = rgb[2];
+    L.term[ray] = term;
+    L.steps[ray] = steps;
+    L.resid[ray] = resid;
+  }
+}
+
+constexpr int TRACE_BLOCK = 128;
+
+// geodesic.rs:62-117 for every ray of the job, persistent over a work queue.
+template <int K, int SRC, int SINK>
+__global__ void __launch_bounds__(TRACE_BLOCK) trace_fp64_kernel(const TraceLaunch L) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int64_t ray = -1;
+  int64_t n = 0;
+  double y[8];
+  bool queue_open = true;
+  bool singular = false;
+  for (;;) {
+    // Refill idle lanes from the queue (one atomic per warp).
+    const unsigned need = __ballot_sync(FULL, ray < 0);
+    if (need && queue_open) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(L.queue, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (base + __popc(need) >= (unsigned long long)L.n) queue_open = false;
+      if (ray < 0) {
+        const unsigned long long idx = base + __popc(need & lt_mask);
+        if (idx < (unsigned long long)L.n) {
+          ray = (int64_t)idx;
+          n = 0;
+          load_ray<SRC>(L, ray, y);
+        }
+      }
+    }
+    if (__ballot_sync(FULL, ray >= 0) == 0) break;
+    if (ray >= 0) {
+      if (n >= L.max_steps) {  // loop exhausted: Diverged with steps_taken = max_steps
+        store_ray<K, SINK>(L, ray, TERM_DIVERGED, y, L.max_steps);
+        ray = -1;
+      } else {
+        const int t = metric_terminate<K>(L.M, y);
+        if (t != TERM_NONE) {
+          store_ray<K, SINK>(L, ray, t, y, n);
+          ray = -1;
+        } else {
+          double yn[8];
+          singular |= !rk4_step<K>(L.M, y, L.step, L.half_step, L.sixth, yn);
+          bool finite = true;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) finite &= isfinite(yn[i]);
+          if (!finite) {
+            store_ray<K, SINK>(L, ray, TERM_DIVERGED, y, n);
+            ray = -1;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) y[i] = yn[i];
+            ++n;
+          }
+        }
+      }
+    }
+  }
+  if (singular) atomicOr(L.flags, 1);
+}
+
+template <int K, int SRC, int SINK>
+static cudaError_t launch_kst(const TraceLaunch& L, cudaStream_t s) {
+  static int grid_cache = 0;
+  if (grid_cache == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_fp64_kernel<K, SRC, SINK>,
+                                                  TRACE_BLOCK, 0);
+    if (per_sm < 1) per_sm = 1;
+    grid_cache = sms * per_sm;
+  }
+  int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
+  int grid = (int)(need < grid_cache ? need : grid_cache);
+  if (grid < 1) grid = 1;
+  trace_fp64_kernel<K, SRC, SINK><<<grid, TRACE_BLOCK, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+template <int K>
+static cudaError_t launch_k(const TraceLaunch& L, int src, int sink, cudaStream_t s) {
+  if (src == SRC_ARRAY && sink == SINK_TRACE) return launch_kst<K, SRC_ARRAY, SINK_TRACE>(L, s);
+  if (src == SRC_CAMERA && sink == SINK_RENDER) return launch_kst<K, SRC_CAMERA, SINK_RENDER>(L, s);
+  if (src == SRC_CAMERA && sink == SINK_TRACE) return launch_kst<K, SRC_CAMERA, SINK_TRACE>(L, s);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStream_t s) {
+  if (L.n <= 0) return cudaSuccess;
+  if (src == SRC_EQUATORIAL) {
+    if (L.M.kind != KIND_SCHWARZSCHILD) return cudaErrorInvalidValue;
+    if (sink == SINK_SHADOW) return launch_kst<KIND_SCHWARZSCHILD, SRC_EQUATORIAL, SINK_SHADOW>(L, s);
+    if (sink == SINK_TRACE) return launch_kst<KIND_SCHWARZSCHILD, SRC_EQUATORIAL, SINK_TRACE>(L, s);
+    return cudaErrorInvalidValue;
+  }
+  switch (L.M.kind) {
+    case KIND_MINKOWSKI: return launch_k<KIND_MINKOWSKI>(L, src, sink, s);
+    case KIND_SCHWARZSCHILD: return launch_k<KIND_SCHWARZSCHILD>(L, src, sink, s);
+    case KIND_ALCUBIERRE: return launch_k<KIND_ALCUBIERRE>(L, src, sink, s);
+    case KIND_MORRIS_THORNE: return launch_k<KIND_MORRIS_THORNE>(L, src, sink, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// Per-pixel reduction of sub-samples (render.rs:77-136) and image statistics
+// (render.rs:146-164). Sub-samples are summed in the reference's (sj, si) order.
+// stats: [captured, escaped, diverged, sum of per-pixel step averages,
+//         max residual bits, sum of all sample steps]
+// ---------------------------------------------------------------------------
+__global__ void render_reduce_kernel(const float* __restrict__ srgb, const int32_t* __restrict__ term,
+                                     const int64_t* __restrict__ steps, const double* __restrict__ resid,
+                                     int64_t npix, int64_t spa, float* __restrict__ rgb,
+                                     int32_t* __restrict__ pclass, int64_t* __restrict__ psteps,
+                                     unsigned long long* __restrict__ stats) {
+  const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int c_cap = 0, c_esc = 0, c_div = 0;
+  unsigned long long pst = 0, tot = 0, rbits = 0;
+  if (pix < npix) {
+    const int64_t spa2 = spa * spa;
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f;
+    int64_t total = 0;
+    double maxr = 0.0;
+    unsigned nc = 0, ne = 0, nd = 0;
+    for (int64_t q = 0; q < spa2; ++q) {
+      const int64_t s = pix * spa2 + q;
+      acc0 += srgb[3 * s];
+      acc1 += srgb[3 * s + 1];
+      acc2 += srgb[3 * s + 2];
+      const int t = term[s];
+      if (t == TERM_CAPTURED) ++nc;
+      else if (t == TERM_DIVERGED) ++nd;
+      else ++ne;
+      total += steps[s];
+      const double r = resid[s];
+      if (isfinite(r) && r > maxr) maxr = r;
+    }
+    const float nf = (float)spa2;
+    rgb[3 * pix] = acc0 / nf;
+    rgb[3 * pix + 1] = acc1 / nf;
+    rgb[3 * pix + 2] = acc2 / nf;
+    int cls;
+    if (nd > 0 && nd >= nc && nd >= ne) cls = TERM_DIVERGED;
+    else if (nc >= ne) cls = TERM_CAPTURED;
+    else cls = TERM_ESCAPED;
+    if (pclass) pclass[pix] = cls;
+    const int64_t ps = total / spa2;
+    if (psteps) psteps[pix] = ps;
+    c_cap = cls == TERM_CAPTURED;
+    c_esc = cls == TERM_ESCAPED;
+    c_div = cls == TERM_DIVERGED;
+    pst = (unsigned long long)ps;
+    tot = (unsigned long long)total;
+    rbits = (unsigned long long)__double_as_longlong(maxr);
+  }
+  // warp reduction, then one atomic per warp
+  const unsigned FULL = 0xffffffffu;
+  for (int o = 16; o > 0; o >>= 1) {
+    c_cap += __shfl_down_sync(FULL, c_cap, o);
+    c_esc += __shfl_down_sync(FULL, c_esc, o);
+    c_div += __shfl_down_sync(FULL, c_div, o);
+    pst += __shfl_down_sync(FULL, pst, o);
+    tot += __shfl_down_sync(FULL, tot, o);
+    const unsigned long long ob = __shfl_down_sync(FULL, rbits, o);
+    rbits = ob > rbits ? ob : rbits;  // non-negative doubles order like their bits
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (c_cap) atomicAdd(&stats[0], (unsigned long long)c_cap);
+    if (c_esc) atomicAdd(&stats[1], (unsigned long long)c_esc);
+    if (c_div) atomicAdd(&stats[2], (unsigned long long)c_div);
+    if (pst) atomicAdd(&stats[3], pst);
+    if (rbits) atomicMax(&stats[4], rbits);
+    if (tot) atomicAdd(&stats[5], tot);
+  }
+}
+
+cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,
+                                 const double* resid, int64_t npix, int64_t spa, float* rgb,
+                                 int32_t* pclass, int64_t* psteps, unsigned long long* stats,
+                                 cudaStream_t s) {
+  if (npix <= 0) return cudaSuccess;
+  const int block = 256;
+  const int64_t grid = (npix + block - 1) / block;
+  render_reduce_kernel<<<(unsigned)grid, block, 0, s>>>(srgb, term, steps, resid, npix, spa, rgb,
+                                                        pclass, psteps, stats);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Point-wise metric functors over n points (AoS in/out).
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void pointwise_kernel(const MetricDesc M, int what, const double* __restrict__ in, int64_t n,
+                                 double* __restrict__ out, int32_t* __restrict__ iout, int* flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (what == PW_ASYM) {
+    const double* s = in + 8 * i;
+    double x[4] = {s[0], s[1], s[2], s[3]}, p[4] = {s[4], s[5], s[6], s[7]}, d[3];
+    metric_asymptotic_direction<K>(x, p, d);
+    out[3 * i] = d[0]; out[3 * i + 1] = d[1]; out[3 * i + 2] = d[2];
+    return;
+  }
+  const double x[4] = {in[4 * i], in[4 * i + 1], in[4 * i + 2], in[4 * i + 3]};
+  if (what == PW_G) {
+    double g[16];
+    metric_g<K>(M, x, g);
+    for (int q = 0; q < 16; ++q) out[16 * i + q] = g[q];
+  } else if (what == PW_GINV) {
+    double g[16];
+    if (!metric_g_inv<K>(M, x, g)) atomicOr(flags, 1);
+    for (int q = 0; q < 16; ++q) out[16 * i + q] = g[q];
+  } else if (what == PW_DG) {
+    double d[64];
+    metric_dg<K>(M, x, d);
+    for (int q = 0; q < 64; ++q) out[64 * i + q] = d[q];
+  } else if (what == PW_CHRISTOFFEL) {
+    double G[64];
+    if (!metric_christoffel<K>(M, x, G)) atomicOr(flags, 1);
+    for (int q = 0; q < 64; ++q) out[64 * i + q] = G[q];
+  } else if (what == PW_TERMINATE) {
+    iout[i] = metric_terminate<K>(M, x);
+  }
+}
+
+cudaError_t launch_pointwise(const MetricDesc& M, int what, const double* in, int64_t n, double* out,
+                             int32_t* iout, int* flags, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int block = 128;
+  const unsigned grid = (unsigned)((n + block - 1) / block);
+  switch (M.kind) {
+    case KIND_MINKOWSKI: pointwise_kernel<KIND_MINKOWSKI><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
+    case KIND_SCHWARZSCHILD: pointwise_kernel<KIND_SCHWARZSCHILD><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
+    case KIND_ALCUBIERRE: pointwise_kernel<KIND_ALCUBIERRE><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
+    case KIND_MORRIS_THORNE: pointwise_kernel<KIND_MORRIS_THORNE><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Camera tetrad by Gram-Schmidt against g (camera.rs:47-97), one thread.
+// status: 0 ok, GEON_ERR_NOT_TIMELIKE, GEON_ERR_GRAM_SCHMIDT.
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void tetrad_kernel(const MetricDesc M, const double* __restrict__ obs, double* __restrict__ out,
+                              int* __restrict__ status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double x[4] = {obs[0], obs[1], obs[2], obs[3]};
+  double g[16];
+  metric_g<K>(M, x, g);
+  double tet[4][4];
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) tet[a][b] = 0.0;
+  *status = 0;
+  const double gtt = g[0];
+  if (!(gtt < 0.0)) {
+    *status = GEON_ERR_NOT_TIMELIKE;
+    for (int q = 0; q < 16; ++q) out[q] = 0.0;
+    return;
+  }
+  tet[0][0] = 1.0 / sqrt(-gtt);
+  for (int i = 0; i < 3; ++i) {
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    v[i + 1] = 1.0;
+    for (int k = 0; k <= i; ++k) {
+      const double proj = dot4(g, tet[k], v);
+      const double norm_k = dot4(g, tet[k], tet[k]);
+      const double coeff = proj / norm_k;
+      for (int mu = 0; mu < 4; ++mu) v[mu] -= coeff * tet[k][mu];
+    }
+    const double n2 = dot4(g, v, v);
+    if (!(n2 > 0.0)) {
+      *status = GEON_ERR_GRAM_SCHMIDT;
+      break;
+    }
+    const double nn = sqrt(n2);
+    for (int mu = 0; mu < 4; ++mu) tet[i + 1][mu] = v[mu] / nn;
+  }
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) out[4 * a + b] = tet[a][b];
+}
+
+cudaError_t launch_tetrad(const MetricDesc& M, const double* obs, double* out16, int* status,
+                          cudaStream_t s) {
+  switch (M.kind) {
+    case KIND_MINKOWSKI: tetrad_kernel<KIND_MINKOWSKI><<<1, 32, 0, s>>>(M, obs, out16, status); break;
+    case KIND_SCHWARZSCHILD: tetrad_kernel<KIND_SCHWARZSCHILD><<<1, 32, 0, s>>>(M, obs, out16, status); break;
+    case KIND_ALCUBIERRE: tetrad_kernel<KIND_ALCUBIERRE><<<1, 32, 0, s>>>(M, obs, out16, status); break;
+    case KIND_MORRIS_THORNE: tetrad_kernel<KIND_MORRIS_THORNE><<<1, 32, 0, s>>>(M, obs, out16, status); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// Derived constants that need the deterministic tanh (alcubierre.rs:42).
+__global__ void metric_init_kernel(MetricDesc* d) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (d->kind == KIND_ALCUBIERRE) d->alc_denom = 2.0 * dm::tanh_det(d->p[0] / d->p[1]);
+}
+
+cudaError_t launch_metric_init(MetricDesc* d_desc, cudaStream_t s) {
+  metric_init_kernel<<<1, 32, 0, s>>>(d_desc);
+  return cudaGetLastError();
+}
+
+__global__ void camera_rays_kernel(const CameraDesc c, double du, double dv, double* __restrict__ out) {
+  const int64_t n = c.width * c.height;
+  const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= n) return;
+  // one sample per pixel at (du, dv): reuse camera_ray's arithmetic with spa = 1
+  const int64_t j = pix / c.width, i = pix - j * c.width;
+  const double u = (2.0 * ((double)i + du) / c.width_d - 1.0) * c.w_img;
+  const double v = -(2.0 * ((double)j + dv) / c.height_d - 1.0) * c.h_img;
+  const double fs = (double)c.forward_sign;
+  const double dx = -fs;
+  const double dy = -v;
+  const double dz = c.forward_sign == 1 ? u : fs * u;
+  const double norm = sqrt(dx * dx + dy * dy + dz * dz);
+  const double n1 = dx / norm, n2 = dy / norm, n3 = dz / norm;
+  double* y = out + 8 * pix;
+  for (int mu = 0; mu < 4; ++mu) y[mu] = c.obs[mu];
+  for (int mu = 0; mu < 4; ++mu)
+    y[4 + mu] = c.tet[0][mu] + n1 * c.tet[1][mu] + n2 * c.tet[2][mu] + n3 * c.tet[3][mu];
+}
+
+cudaError_t launch_camera_rays(const CameraDesc& c, double du, double dv, double* out, cudaStream_t s) {
+  const int64_t n = c.width * c.height;
+  if (n <= 0) return cudaSuccess;
+  camera_rays_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(c, du, dv, out);
+  return cudaGetLastError();
+}
+
+__global__ void equatorial_rays_kernel(double m, double r_obs, const double* __restrict__ alpha, int64_t n,
+                                       double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double y[8];
+  equatorial_ray(m, r_obs, alpha[i], y);
+  for (int q = 0; q < 8; ++q) out[8 * i + q] = y[q];
+}
+
+cudaError_t launch_equatorial_rays(double m, double r_obs, const double* alpha, int64_t n, double* out,
+                                   cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  equatorial_rays_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(m, r_obs, alpha, n, out);
+  return cudaGetLastError();
+}
+
+__global__ void sky_kernel(const double* __restrict__ dir, int64_t n, int show, float* __restrict__ rgb) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d[3] = {dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]};
+  float c[3];
+  sky_sample(d, show != 0, c);
+  rgb[3 * i] = c[0]; rgb[3 * i + 1] = c[1]; rgb[3 * i + 2] = c[2];
+}
+
+cudaError_t launch_sky(const double* dir, int64_t n, int show, float* rgb, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  sky_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dir, n, show, rgb);
+  return cudaGetLastError();
+}
+
+}  // namespace geon

@@ -1,0 +1,58 @@
+"""curvature.rs (Riemann -> Ricci -> R -> Einstein -> T -> T(k,k)) on the GPU, FP64."""
+import numpy as np
+
+from . import _ffi
+from ._util import check, dp, f64, points
+
+
+def _call(fn, metric, x, shape):
+    a, single = points(x, 4)
+    n = a.shape[0]
+    out = np.empty((n,) + shape)
+    check(getattr(_ffi.load(), fn)(metric.handle, dp(a), n, dp(out)))
+    return out[0] if single else out
+
+
+def riemann(metric, x):
+    """R^rho_{sigma mu nu} as [rho][sigma][mu][nu] (curvature.rs:48-70)."""
+    return _call("geon_riemann", metric, x, (4, 4, 4, 4))
+
+
+def ricci(metric, x):
+    return _call("geon_ricci", metric, x, (4, 4))
+
+
+def ricci_scalar(metric, x):
+    r = _call("geon_ricci_scalar", metric, x, ())
+    return float(r) if np.ndim(r) == 0 else r
+
+
+def einstein(metric, x):
+    return _call("geon_einstein", metric, x, (4, 4))
+
+
+def stress_energy(metric, x):
+    return _call("geon_stress_energy", metric, x, (4, 4))
+
+
+def nec_contraction(metric, x, k):
+    """T_mu_nu k^mu k^nu. k: (4,) or (nk, 4) shared by all points, or (n, nk, 4)."""
+    a, single = points(x, 4)
+    n = a.shape[0]
+    kk = np.asarray(k, dtype=np.float64)
+    k_single = kk.ndim == 1
+    if kk.ndim <= 2:
+        kk = f64(kk.reshape(-1, 4))
+        nk, shared = kk.shape[0], 1
+    else:
+        kk = f64(kk)
+        nk, shared = kk.shape[1], 0
+    out = np.empty((n, nk))
+    check(_ffi.load().geon_nec_contraction(metric.handle, dp(a), n, dp(kk), nk, shared, dp(out)))
+    if k_single:
+        out = out[:, 0]
+    return (float(out[0]) if k_single else out[0]) if single else out
+
+
+def wec_contraction(metric, x, u):
+    return nec_contraction(metric, x, u)

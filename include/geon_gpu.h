@@ -1,0 +1,193 @@
+/*
+ * geon_gpu.h: C ABI of the GB300 geodesic ray-tracing and curvature library.
+ *
+ * A drop-in for the hot path of the geon crate (Rust): the Metric trait's
+ * functors with their finite-difference fallbacks, geodesic::trace, the Camera
+ * tetrad, render(), the shadow bisection of bin/validate_shadow.rs and the
+ * curvature.rs chain. A Rust host binds these with `extern "C"` declarations
+ * (INTEGRATION.md shows the shim); every array layout below is the memory layout
+ * of the corresponding Rust type, so slices pass through without copies:
+ *   Vec4 = [f64; 4], Mat4 = [[f64; 4]; 4] (row-major), Christoffel =
+ *   [[[f64; 4]; 4]; 4] indexed [mu][alpha][beta], State = [f64; 8] =
+ *   (x^0..x^3, p^0..p^3), Riemann = [[[[f64; 4]; 4]; 4]; 4] indexed
+ *   [rho][sigma][mu][nu].
+ *
+ * Conventions
+ *  - Every function returns GEON_OK (0) or a negative GEON_ERR_* status; where
+ *    the reference panics (singular metric, non-timelike observer, failed
+ *    Gram-Schmidt) the call returns the matching status and the host shim
+ *    raises the reference's panic message. geon_last_error() gives a message.
+ *  - Plain entry points take HOST pointers, copy in, run, copy out and return
+ *    when the results are in the caller's buffers. `_dev` variants take DEVICE
+ *    pointers and a cudaStream_t (as void*) and are stream-ordered.
+ *  - Handles are immutable after creation; calls are thread-safe.
+ *  - Termination codes: GEON_DIVERGED 0, GEON_CAPTURED 1, GEON_ESCAPED 2 (the
+ *    encoding of the reference's cuda/schwarzschild_render.cu:93); -1 = None.
+ *  - precision: GEON_FP64 reproduces the reference's FP64 arithmetic (the same
+ *    bits as the reference for the same sin/cos/tanh values); GEON_MIXED runs
+ *    the FP32 bulk integrator with FP64 kept where stability needs it.
+ */
+#ifndef GEON_GPU_H
+#define GEON_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GEON_ABI_VERSION 1
+
+/* status codes */
+#define GEON_OK 0
+#define GEON_ERR_INVALID (-1)          /* bad argument */
+#define GEON_ERR_SINGULAR_METRIC (-2)  /* types.rs:39 panic: g not invertible */
+#define GEON_ERR_NOT_TIMELIKE (-3)     /* camera.rs:53 panic: g_tt >= 0 at the observer */
+#define GEON_ERR_GRAM_SCHMIDT (-4)     /* camera.rs:85-88 panic: n^2 <= 0 */
+#define GEON_ERR_CUDA (-5)             /* CUDA runtime error */
+#define GEON_ERR_OOM (-6)              /* device allocation failed */
+#define GEON_ERR_ADMISSION (-7)        /* job larger than the server's memory budget */
+#define GEON_ERR_TIMEOUT (-8)          /* wait deadline passed */
+#define GEON_ERR_NOT_FOUND (-9)        /* unknown job id */
+#define GEON_ERR_CANCELLED (-10)       /* job cancelled */
+#define GEON_ERR_UNSUPPORTED (-11)     /* combination not provided */
+
+enum geon_metric_kind {
+  GEON_MINKOWSKI = 0,     /* metric/minkowski.rs */
+  GEON_SCHWARZSCHILD = 1, /* metric/schwarzschild.rs */
+  GEON_ALCUBIERRE = 2,    /* metric/alcubierre.rs */
+  GEON_MORRIS_THORNE = 3  /* metric/morris_thorne.rs */
+};
+enum geon_termination { GEON_DIVERGED = 0, GEON_CAPTURED = 1, GEON_ESCAPED = 2 };
+enum geon_precision { GEON_FP64 = 0, GEON_MIXED = 1 };
+
+typedef struct geon_metric* geon_metric_t;
+
+/* Camera (camera.rs:21-36). forward_sign = +1 is the reference camera (image
+ * forward = -e1, right = +e3, up = -e2); -1 looks along +e1 with right = -e3,
+ * an extension for poses the reference camera cannot express. */
+typedef struct {
+  double observer[4];
+  double fov_y_deg;
+  int64_t width;
+  int64_t height;
+  int32_t forward_sign;
+  int32_t reserved;
+} geon_camera;
+
+/* RenderConfig (render.rs:17-43) plus the sky flag and precision. */
+typedef struct {
+  double step;              /* default 0.05 */
+  int64_t max_steps;        /* default 20000 */
+  float captured_rgb[3];    /* default (0, 0, 0) */
+  float diverged_rgb[3];    /* default (1, 0, 1) */
+  int64_t samples_per_axis; /* default 1 */
+  int32_t show_stars;       /* 1/0, or -1 to use the process-wide flag (sky.rs:23) */
+  int32_t precision;        /* GEON_FP64 or GEON_MIXED */
+} geon_render_config;
+
+/* RenderStats (render.rs:45-53) plus the total ray-step count. */
+typedef struct {
+  int64_t captured;
+  int64_t escaped;
+  int64_t diverged;
+  double max_null_residual;
+  double avg_steps;
+  int64_t total_steps; /* sum of steps_taken over every traced sample */
+} geon_render_stats;
+
+const char* geon_version(void);
+/* Message of the last failed call on this thread. */
+const char* geon_last_error(void);
+/* Fill cfg with RenderConfig::default() (render.rs:32-43). */
+void geon_render_config_default(geon_render_config* cfg);
+
+/* --- Metric handles (trait Metric, metric/mod.rs:19; the four `impl Metric` blocks) --
+ * params, by kind (the reference struct's fields in declaration order):
+ *   MINKOWSKI      none
+ *   SCHWARZSCHILD  {mass, horizon_pad, escape_radius}  (Schwarzschild::new(m): pad 1.001, escape 1000)
+ *   ALCUBIERRE     {bubble_radius, bubble_thickness, ship_velocity, ship_x}
+ *   MORRIS_THORNE  {throat_radius}
+ * Missing trailing params take the reference's defaults. */
+int geon_metric_create(int kind, const double* params, int nparams, geon_metric_t* out);
+int geon_metric_destroy(geon_metric_t m);
+int geon_metric_kind(geon_metric_t m);
+/* Metric::name (metric/mod.rs:84) */
+const char* geon_metric_name(geon_metric_t m);
+
+/* Point-wise functors over n points. x: n Vec4. */
+int geon_metric_g(geon_metric_t m, const double* x, size_t n, double* out_mat4);          /* Metric::g, mod.rs:21 (n*16) */
+int geon_metric_dg(geon_metric_t m, const double* x, size_t n, double* out_dg);           /* Metric::dg, mod.rs:25-43, [alpha][mu][nu] (n*64) */
+int geon_metric_g_inv(geon_metric_t m, const double* x, size_t n, double* out_mat4);      /* Metric::g_inv, mod.rs:46-48 (n*16) */
+int geon_metric_christoffel(geon_metric_t m, const double* x, size_t n, double* out_chr); /* Metric::christoffel, mod.rs:51-69 (n*64) */
+int geon_metric_terminate(geon_metric_t m, const double* x, size_t n, int32_t* out_term); /* Metric::terminate, mod.rs:78, -1 = None */
+/* Metric::asymptotic_direction (mod.rs:91-108) over n States: n*3 out. */
+int geon_metric_asymptotic_direction(geon_metric_t m, const double* states, size_t n, double* out_dir);
+
+/* --- geodesic::trace (geodesic.rs:62-117) over n rays ----------------------
+ * y0: n States. Outputs (each may be NULL except term): termination, final
+ * State, steps_taken, null_residual. precision: GEON_FP64 or GEON_MIXED. */
+int geon_trace(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps,
+               int precision, int32_t* term, double* final_state, int64_t* steps_taken,
+               double* null_residual);
+int geon_trace_dev(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps,
+                   int precision, int32_t* term, double* final_state, int64_t* steps_taken,
+                   double* null_residual, void* stream);
+
+/* --- Camera (camera.rs:47-160) --------------------------------------------- */
+/* Camera::tetrad (camera.rs:47-97): rows e_(a)^mu, out 16 doubles. */
+int geon_camera_tetrad(geon_metric_t m, const double observer[4], double out_tetrad[16]);
+/* Camera::ray_state_sub (camera.rs:113-160) for every pixel at sub-pixel (du, dv):
+ * out width*height States, row-major (pixel (i, j) at j*width + i). */
+int geon_camera_ray_states(const geon_camera* cam, const double tetrad[16], double du, double dv,
+                           double* out_states);
+
+/* --- render() (render.rs:55-166) ------------------------------------------- */
+/* rgb: width*height*3 floats, row-major, top-left origin (the Vec<f32>). */
+int geon_render(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
+                geon_render_stats* stats);
+/* As geon_render, also returning per-pixel classification (render.rs:129-135)
+ * and per-pixel mean steps; either may be NULL. */
+int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg,
+                   float* rgb, geon_render_stats* stats, int32_t* pixel_class,
+                   int64_t* pixel_steps);
+/* sky::sample (sky.rs:107-120) over n unit directions (n*3 in, n*3 out). */
+int geon_sky_sample(const double* dir, size_t n, int show_stars, float* rgb);
+/* sky::SHOW_STARS (sky.rs:23; set by bin/render.rs:71-73). */
+void geon_set_show_stars(int on);
+int geon_get_show_stars(void);
+
+/* --- curvature.rs ------------------------------------------------------------ */
+int geon_riemann(geon_metric_t m, const double* x, size_t n, double* out);       /* curvature.rs:48, n*256 */
+int geon_ricci(geon_metric_t m, const double* x, size_t n, double* out);         /* curvature.rs:72, n*16 */
+int geon_ricci_scalar(geon_metric_t m, const double* x, size_t n, double* out);  /* curvature.rs:87, n */
+int geon_einstein(geon_metric_t m, const double* x, size_t n, double* out);      /* curvature.rs:99, n*16 */
+int geon_stress_energy(geon_metric_t m, const double* x, size_t n, double* out); /* curvature.rs:112, n*16 */
+/* nec_contraction (curvature.rs:127-136) at n points for nk vectors each: k is nk Vec4 shared by all
+ * points when k_shared != 0, else n*nk Vec4 (point-major). out: n*nk. */
+int geon_nec_contraction(geon_metric_t m, const double* x, size_t n, const double* k, size_t nk,
+                         int k_shared, double* out);
+/* wec_contraction is nec_contraction with a timelike vector (curvature.rs:139-141). */
+int geon_wec_contraction(geon_metric_t m, const double* x, size_t n, const double* u, size_t nu,
+                         int u_shared, double* out);
+
+/* --- shadow validation (bin/validate_shadow.rs:20-94) ------------------------ */
+/* equatorial_ray (validate_shadow.rs:20-35): n launch angles -> n States. */
+int geon_equatorial_rays(geon_metric_t schwarzschild, double r_obs, const double* alpha, size_t n,
+                         double* out_states);
+/* is_captured (validate_shadow.rs:37-41) for n launch angles: term (n), steps (n, may be NULL). */
+int geon_shadow_classify(geon_metric_t schwarzschild, double r_obs, const double* alpha, size_t n,
+                         double step, int64_t max_steps, int precision, int32_t* term,
+                         int64_t* steps);
+/* nb independent bisections of `iters` halvings each on [lo[i], hi[i]]
+ * (bin/validate_shadow.rs:70-79). Outputs alpha_c = 0.5*(lo+hi) after the loop;
+ * lo_out/hi_out/steps_out (ray-steps spent) may be NULL. With GEON_FP64 the
+ * result equals the sequential bisection bit for bit. */
+int geon_shadow_bisect(geon_metric_t schwarzschild, double r_obs, const double* lo, const double* hi,
+                       size_t nb, int iters, double step, int64_t max_steps, int precision,
+                       double* alpha_c, double* lo_out, double* hi_out, int64_t* steps_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GEON_GPU_H */

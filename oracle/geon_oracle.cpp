@@ -117,7 +117,7 @@ void geon_sincos(double x, double* sp, double* cp) {
   const double wc = 1.0 - hz;
   const double zl = std::fma(t, t, -z);            // exact error of z
   const double cv = wc + (((1.0 - wc) - hz) + (std::fma(z * z, pc, -0.5 * zl) - tl * t));
-  const double q = k - 4.0 * std::floor(k * 0.25);  // k mod 4, exact
+  const double q = k - 4.0 * std::floor(k * 0.25);  // k mod 4 in [0, 4), exact for every finite k
   if (q == 0.0) { *sp = sv; *cp = cv; }
   else if (q == 1.0) { *sp = cv; *cp = -sv; }
   else if (q == 2.0) { *sp = -sv; *cp = -cv; }

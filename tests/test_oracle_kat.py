@@ -1,0 +1,118 @@
+"""Pin the CPU oracle to the reference's own known answers (CPU only).
+
+The reference has no test suite; its validation is the printed output of
+bin/energy_conditions.rs (committed as docs/energy_conditions.txt) and of
+bin/validate_shadow.rs (quoted in README.md:43-50). tests/golden/ holds those
+numbers; the oracle must reproduce every printed digit.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def fmt(v):
+    # Rust's {:+.4e} prints e.g. +1.7073e-3 / -2.4626e-2 / +0.0000e0
+    s = "%+.4e" % v
+    mant, exp = s.split("e")
+    return f"{mant}e{int(exp)}"
+
+
+def golden_values(ec):
+    vals = [r["value"] for r in ec["minkowski"]] + [r["value"] for r in ec["schwarzschild"]]
+    return vals
+
+
+@pytest.mark.parametrize("math", [0, 1], ids=["libm", "geon"])
+def test_energy_conditions_printed_digits(orc, math):
+    ec = json.load(open(os.path.join(GOLD, "energy_conditions.json"), encoding="utf-8"))
+    out = orc.energy_conditions(math)
+    assert len(out) == 99
+    got_mink = out[0:2]
+    got_schw = out[2:8]
+    alc = out[8:49]
+    mt = out[52:93]
+    pairs = list(zip(got_mink, [r["value"] for r in ec["minkowski"]]))
+    pairs += list(zip(got_schw, [r["value"] for r in ec["schwarzschild"]]))
+    pairs += list(zip(alc[::4], [r["value"] for r in ec["alcubierre"]]))
+    pairs += list(zip(mt[::4], [r["value"] for r in ec["morris_thorne"]]))
+    pairs += [(out[49], ec["alcubierre_min"]), (out[51], ec["alcubierre_integral"]),
+              (out[93], ec["morris_thorne_min"])]
+    pairs += list(zip(out[95:99], ec["morris_thorne_throat_T_diag"]))
+    assert len(pairs) == 2 + 6 + 11 + 11 + 3 + 4
+    for got, want in pairs:
+        assert fmt(got) == fmt(want), (got, want)
+    # "at x = {:.2}": the minimum sits at x = +2.40 (not -2.40) in the reference's run
+    assert "%.2f" % out[50] == "%.2f" % ec["alcubierre_min_at"]
+    assert "%.2f" % out[94] == "%.2f" % ec["morris_thorne_min_at"]
+    # Morris-Thorne throat: T_tt = -1/(8 pi) to the printed digits (README.md:72)
+    assert fmt(out[95]) == fmt(-1.0 / (8.0 * np.pi))
+
+
+@pytest.mark.parametrize("math", [0, 1], ids=["libm", "geon"])
+def test_validate_shadow_b_c(orc, math):
+    g = json.load(open(os.path.join(GOLD, "validate_shadow.json"), encoding="utf-8"))
+    ac, lo, hi, st = orc.shadow_bisect([1.0, 1.001, 1000.0], 20.0, [0.0], [np.pi / 2 - 1e-3], 60, 0.01,
+                                       200000, math=math)
+    f = 1.0 - 2.0 / 20.0
+    b_c = 20.0 * np.sin(ac[0]) / np.sqrt(f)
+    b_an = np.sqrt(3.0) * 3.0
+    assert "%.6f" % b_c == "%.6f" % g["b_c_measured"]
+    assert "%.4f" % np.degrees(ac[0]) == "%.4f" % g["alpha_c_measured_deg"]
+    assert "%.2e" % (abs(b_c - b_an) / b_an) == "%.2e" % g["rel_err"]
+
+
+def test_minkowski_null_residual(orc):
+    # README.md:50: Minkowski rays stay on the null cone to ~5e-16.
+    rc, tet = orc.camera_tetrad(0, [], [0.0, 20.0, 0.0, 0.0])
+    assert rc == 0
+    y0 = orc.camera_rays(tet, [0.0, 20.0, 0.0, 0.0], 60.0, 16, 16)
+    # from r = 20 through the origin to r > 1000 takes > 20000 steps of 0.05
+    term, yf, steps, resid = orc.trace(0, [], y0, 0.05, 30000)
+    assert np.all(term == 2)
+    assert resid.max() < 2e-15
+
+
+def test_inv4_matches_linear_algebra(orc):
+    rng = np.random.default_rng(1)
+    for _ in range(200):
+        m = rng.normal(size=(4, 4)) + 4 * np.eye(4)
+        inv = orc.inv4(m)
+        np.testing.assert_allclose(inv, np.linalg.inv(m), rtol=1e-11, atol=1e-13)
+    assert orc.inv4(np.zeros((4, 4))) is None
+
+
+def test_geon_math_close_to_libm(orc):
+    rng = np.random.default_rng(2)
+    x = np.concatenate([rng.uniform(-60, 60, 100000), rng.uniform(1.55, 1.6, 20000), [np.pi / 2, 0.0]])
+    s, c = orc.geon_sincos(x)
+    us = np.abs(s.view(np.int64) - np.sin(x).view(np.int64))
+    uc = np.abs(c.view(np.int64) - np.cos(x).view(np.int64))
+    assert us.max() <= 1 and uc.max() <= 1
+    assert (us == 0).mean() > 0.97 and (uc == 0).mean() > 0.97
+    assert c[-2] == np.cos(np.pi / 2)  # 6.123233995736766e-17, as glibc
+    t = rng.uniform(-25, 25, 100000)
+    ut = np.abs(orc.geon_tanh(t).view(np.int64) - np.tanh(t).view(np.int64))
+    assert ut.max() <= 3
+
+
+def test_math_mode_floor(orc):
+    """A 1-ulp change in libm moves the FD curvature of the reference by ~1e-7:
+    the geon-math oracle sits inside that floor."""
+    a = orc.energy_conditions(0)
+    b = orc.energy_conditions(1)
+    c = orc.energy_conditions(2)
+    floor = np.abs(a - c).max()
+    assert 1e-9 < floor < 1e-6
+    assert np.abs(a - b).max() <= 2 * floor
+
+
+def test_faithful_curvature_equals_single_riemann(orc):
+    x = np.array([[0.0, 2.3, 0.4, -0.2], [0.0, -1.7, 0.1, 0.9]])
+    k = np.array([[1.0, 1.0, 0.0, 0.0], [1.0, 0.0, 1.0, 0.0]])
+    a = orc.nec(2, [2.0, 0.5, 2.0, 0.0], x, k, math=0, faithful=True)
+    b = orc.nec(2, [2.0, 0.5, 2.0, 0.0], x, k, math=0, faithful=False)
+    assert np.array_equal(a, b)
