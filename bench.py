@@ -1,0 +1,394 @@
+"""Benchmark: Schwarzschild shadow sweep + concurrent bisections (ray-steps/s).
+
+Workload (one step), Schwarzschild M = 1 (horizon_pad 1.001, escape_radius 1000),
+observer r_obs = 20M, RK4 step 0.01, cap 200,000 steps (bin/validate_shadow.rs
+settings):
+  * sweep: 2^20 equatorial rays with launch angle alpha ~ U[10 deg, 20 deg]
+    (seeded), each classified captured / escaped;
+  * 64 concurrent 40-iteration bisections of alpha_c from seeded brackets
+    lo ~ U[13, 14] deg, hi ~ U[14.5, 15.5] deg.
+At r_obs = 20M the critical angle is 14.269 deg, inside both ranges (at 30M it
+would be 9.63 deg, outside them). Inputs are synthetic and seeded.
+
+value = useful ray-steps (sweep steps + the bisections' sequential-path steps)
+per second of device time with inputs resident in HBM. The default precision
+is the mixed FP32/FP64 path; the plain FP64 path is measured beside it on a
+uniform 1/32 sample of the sweep, and accuracy of mixed vs FP64 is reported.
+`--impl reference` times the CPU restatement of the reference (oracle/) on
+the host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+R_OBS = 20.0
+STEP = 0.01
+MAX_STEPS = 200000
+N_SWEEP = 1 << 20
+N_BRACKETS = 64
+ITERS = 40
+SCHW = [1.0, 1.001, 1000.0]
+ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
+B_C = 3.0 * np.sqrt(3.0)
+
+
+def workload(seed):
+    rng = np.random.default_rng(seed)
+    alpha = np.radians(rng.uniform(10.0, 20.0, N_SWEEP))
+    lo = np.radians(rng.uniform(13.0, 14.0, N_BRACKETS))
+    hi = np.radians(rng.uniform(14.5, 15.5, N_BRACKETS))
+    return alpha, lo, hi
+
+
+def b_of(alpha):
+    return R_OBS * np.sin(alpha) / np.sqrt(1.0 - 2.0 / R_OBS)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+                power.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [s for s in sm if s > 0.5 * max(sm)]
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": max(smax), "samples": len(sm),
+                "power_w_max": max(power), "reasons": sorted(reasons)}
+
+
+def cpu_sample_rate(orc, alpha, n, threads):
+    """Oracle (CPU restatement of the reference) on a uniform sample of the sweep."""
+    sample = alpha[:: max(1, len(alpha) // n)][:n]
+    t0 = time.perf_counter()
+    term, steps = orc.shadow_classify(SCHW, R_OBS, sample, STEP, MAX_STEPS, math=orc.LIBM, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return float(steps.sum()) / dt, dt, int(steps.sum()), len(sample)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    alpha, lo, hi = workload(0x5EED)
+    threads = orc.hardware_threads()
+    n = args.cpu_rays
+    rates = []
+    for i in range(args.warmup + args.steps):
+        rate, dt, st, ns = cpu_sample_rate(orc, np.roll(alpha, 7919 * i), n, threads)
+        if i >= args.warmup:
+            rates.append((rate, dt, st))
+    value = float(sum(r[2] for r in rates) / sum(r[1] for r in rates))
+    line = {
+        "impl": "reference", "metric": "ray-steps/s", "value": value, "unit": "ray-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * float(np.mean([r[1] for r in rates])), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "schwarzschild shadow sweep (2^20 equatorial rays, alpha~U[10,20] deg, r_obs 20M, "
+                               "h 0.01, cap 200000) + 64x40 bisections; reference arm: bounded uniform sample "
+                               f"of {n} sweep rays per step", "rays_per_step": n},
+        "cpu_baseline": {"value": value, "unit": "ray-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} rays per step, uniform over the 2^20-ray sweep"},
+        "e2e": {"value": value, "unit": "ray-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-rays", type=int, default=4096)
+    ap.add_argument("--fp64-sample", type=int, default=32, help="FP64 leg traces every k-th sweep ray")
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 leg, accuracy, e2e and CPU legs")
+    args = ap.parse_args()
+    assert args.warmup >= 3, "at least 3 warm-up steps"
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import geon_gb300 as geon
+    from geon_gb300 import _ffi
+    lib = _ffi.load()
+    prec = 1 if args.precision == "mixed" else 0
+    m = geon.Schwarzschild(*SCHW)
+    h = m.handle
+    alpha, lo, hi = workload(0x5EED + rank)
+    dev = torch.device("cuda", local)
+    d_alpha = torch.tensor(alpha, device=dev)
+    d_lo = torch.tensor(lo, device=dev)
+    d_hi = torch.tensor(hi, device=dev)
+    d_term = torch.empty(N_SWEEP, dtype=torch.int32, device=dev)
+    d_steps = torch.empty(N_SWEEP, dtype=torch.int64, device=dev)
+    d_ac = torch.empty(N_BRACKETS, dtype=torch.float64, device=dev)
+    d_bst = torch.empty(N_BRACKETS, dtype=torch.int64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    sa, sb = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+
+    def check(rc):
+        if rc != 0:
+            raise RuntimeError(lib.geon_last_error().decode())
+
+    def one_step(precision):
+        main = torch.cuda.current_stream()
+        e0 = torch.cuda.Event(enable_timing=True)
+        ea0, ea1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        eb0, eb1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(main)
+        sa.wait_stream(main)
+        sb.wait_stream(main)
+        ea0.record(sa)
+        check(lib.geon_shadow_classify_dev(h, R_OBS, d_alpha.data_ptr(), N_SWEEP, STEP, MAX_STEPS, precision,
+                                           d_term.data_ptr(), d_steps.data_ptr(), sa.cuda_stream))
+        ea1.record(sa)
+        eb0.record(sb)
+        check(lib.geon_shadow_bisect_dev(h, R_OBS, d_lo.data_ptr(), d_hi.data_ptr(), N_BRACKETS, ITERS, STEP,
+                                         MAX_STEPS, precision, d_ac.data_ptr(), None, None, d_bst.data_ptr(),
+                                         sb.cuda_stream))
+        eb1.record(sb)
+        main.wait_stream(sa)
+        main.wait_stream(sb)
+        e1.record(main)
+        return e0, e1, ea0, ea1, eb0, eb1
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        one_step(prec)
+        flush.zero_()
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = lib.geon_launch_count()
+    times, sweep_ms, bis_ms, total_steps = [], [], [], 0
+    barrier()
+    for _ in range(args.steps):
+        ev = one_step(prec)
+        torch.cuda.synchronize()
+        times.append(ev[0].elapsed_time(ev[1]))
+        sweep_ms.append(ev[2].elapsed_time(ev[3]))
+        bis_ms.append(ev[4].elapsed_time(ev[5]))
+        total_steps += int(d_steps.sum().item()) + int(d_bst.sum().item())
+        flush.zero_()  # between timed iterations, outside the events
+    barrier()
+    launches = lib.geon_launch_count() - launches0
+    clocks = sampler.stop()
+    t_total = sum(times) / 1e3
+    if dist is not None:
+        tt = torch.tensor([t_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+        st = torch.tensor([total_steps], dtype=torch.float64, device=dev)
+        dist.all_reduce(st)
+        total_steps = int(st.item())
+    value = total_steps / t_total
+    sweep_steps = int(d_steps.sum().item())
+    sweep_term = d_term.cpu().numpy()
+    ac_mixed = d_ac.cpu().numpy()
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    extras = {}
+    peak32 = ctypes_peak(lib, 0)
+    peak64 = ctypes_peak(lib, 1)
+    kernel_s = float(np.mean(sweep_ms)) / 1e3
+    achieved = ALG_FLOPS_PER_STEP * sweep_steps / kernel_s / 1e12
+    peak = peak32 if prec == 1 else peak64
+    traffic = load_traffic()
+    roofline = {"bound": "fp32 pipe" if prec == 1 else "fp64 pipe", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "kernel": "trace_mixed_kernel<Schwarzschild, equatorial, shadow>" if prec == 1 else
+                "trace_fp64_kernel<Schwarzschild, equatorial, shadow>",
+                "alg_flops_per_ray_step": ALG_FLOPS_PER_STEP,
+                "peak_source": "measured in this run: FFMA/DFMA throughput probe (geon_probe_fma_peak); "
+                               "MEASURED_PEAKS.json has no FP32/FP64 non-tensor peak"}
+
+    if not args.no_extras:
+        extras = extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_mixed, prec, dev, value)
+
+    line = {
+        "metric": "ray-steps/s", "value": value, "unit": "ray-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 with f64 band (mixed)" if prec == 1 else "f64",
+        "data": "synthetic (seeded alpha and brackets)",
+        "config": {"workload": "schwarzschild shadow sweep: 2^20 equatorial rays alpha~U[10,20] deg + 64 concurrent "
+                               "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
+                   "precision": args.precision, "rays_per_gpu": N_SWEEP, "bisections_per_gpu": N_BRACKETS,
+                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards"},
+        "latency": {"bisection_ms_p50": float(np.percentile(bis_ms, 50)),
+                    "bisection_ms_p99": float(np.percentile(bis_ms, 99)),
+                    "sweep_ms_p50": float(np.percentile(sweep_ms, 50)),
+                    "sweep_ms_p99": float(np.percentile(sweep_ms, 99))},
+        "roofline": roofline,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    line.update(extras)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def ctypes_peak(lib, fp64):
+    import ctypes
+    v = ctypes.c_double(0.0)
+    rc = lib.geon_probe_fma_peak(fp64, ctypes.byref(v))
+    return v.value if rc == 0 else None
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(p))
+        return d.get("trace_mixed_shadow_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_run, prec, dev, value):
+    import torch
+    out = {}
+    # FP64 path on a uniform sample of the sweep, and the FP64 bisections.
+    k = args.fp64_sample
+    sample = alpha[::k]
+    t0 = time.perf_counter()
+    t64, s64 = geon.shadow.classify(m, R_OBS, sample, STEP, MAX_STEPS, precision="fp64")
+    dt64 = time.perf_counter() - t0
+    tm, sm = geon.shadow.classify(m, R_OBS, sample, STEP, MAX_STEPS, precision="mixed")
+    ac64, _, _, _ = geon.shadow.bisect(m, R_OBS, lo, hi, ITERS, STEP, MAX_STEPS, precision="fp64")
+    acm, _, _, _ = geon.shadow.bisect(m, R_OBS, lo, hi, ITERS, STEP, MAX_STEPS, precision="mixed")
+    fp64_rate = float(s64.sum()) / dt64
+    mism = float(np.mean(t64 != tm))
+    out["fp64_path"] = {"value": fp64_rate, "unit": "ray-steps/s",
+                        "sample": f"every {k}th sweep ray ({len(sample)} rays), host API wall time",
+                        "mixed_over_fp64": value / fp64_rate}
+    # null drift and direction error on escaped rays (mixed vs FP64 final states)
+    y0 = geon.shadow.equatorial_ray(m, R_OBS, sample[:4096])
+    r64 = geon.trace(m, y0, STEP, MAX_STEPS, precision="fp64")
+    rmx = geon.trace(m, y0, STEP, MAX_STEPS, precision="mixed")
+    esc = (r64.termination == 2) & (rmx.termination == 2)
+    d64 = m.asymptotic_direction(r64.final_state[esc])
+    dmx = m.asymptotic_direction(rmx.final_state[esc])
+    ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0))
+    out["accuracy"] = {
+        "class_mismatch_vs_fp64": mism, "mismatch_sample_rays": int(len(sample)),
+        "b_c_rel_err_mixed_max": float(np.max(np.abs(b_of(acm) - B_C) / B_C)),
+        "b_c_rel_err_fp64_max": float(np.max(np.abs(b_of(ac64) - B_C) / B_C)),
+        "b_c_mixed_minus_fp64_rel_max": float(np.max(np.abs(b_of(acm) - b_of(ac64)) / B_C)),
+        "b_c_this_run_rel_err_max": float(np.max(np.abs(b_of(ac_run) - B_C) / B_C)),
+        "escape_dir_angle_err_rad_max": float(ang.max()) if ang.size else None,
+        "escape_dir_angle_err_rad_p50": float(np.median(ang)) if ang.size else None,
+        "null_drift_max_mixed": float(np.nanmax(rmx.null_residual)),
+        "null_drift_max_fp64": float(np.nanmax(r64.null_residual)),
+    }
+    # e2e: the public host API, pinned host buffers, copies inside the timed region
+    pa = torch.tensor(alpha).pin_memory().numpy()
+    plo = torch.tensor(lo).pin_memory().numpy()
+    phi = torch.tensor(hi).pin_memory().numpy()
+    prec_name = "mixed" if prec == 1 else "fp64"
+    res = {}
+
+    def sweep():
+        res["sweep"] = geon.shadow.classify(m, R_OBS, pa, STEP, MAX_STEPS, precision=prec_name)
+
+    def bis():
+        res["bis"] = geon.shadow.bisect(m, R_OBS, plo, phi, ITERS, STEP, MAX_STEPS, precision=prec_name)
+
+    e2e_times, e2e_steps = [], 0
+    for i in range(2):
+        t0 = time.perf_counter()
+        th = threading.Thread(target=bis)
+        th.start()
+        sweep()
+        th.join()
+        dt = time.perf_counter() - t0
+        if i == 1:
+            e2e_times.append(dt)
+            e2e_steps = int(res["sweep"][1].sum()) + int(res["bis"][3].sum())
+    out["e2e"] = {"value": e2e_steps / float(np.mean(e2e_times)), "unit": "ray-steps/s",
+                  "h2d_bytes_per_step": N_SWEEP * 8 + 2 * N_BRACKETS * 8,
+                  "d2h_bytes_per_step": N_SWEEP * (4 + 8) + N_BRACKETS * (8 * 3 + 8),
+                  "api": "geon_shadow_classify + geon_shadow_bisect (host pointers, two threads)"}
+    # CPU baseline: the oracle (CPU restatement of the reference) on the host cores
+    from oracle import oracle as orc
+    threads = orc.hardware_threads()
+    rate, dt, st, ns = cpu_sample_rate(orc, alpha, args.cpu_rays, threads)
+    out["cpu_baseline"] = {"value": rate, "unit": "ray-steps/s", "cores": threads, "kind": "port",
+                           "sample": f"{ns} rays uniform over the sweep ({st} ray-steps, {dt:.1f} s)"}
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -78,6 +78,9 @@ SIGNATURES = {
     "geon_sky_sample": (ctypes.c_int, [c_double_p, c_size_t, ctypes.c_int, c_float_p]),
     "geon_set_show_stars": (None, [ctypes.c_int]),
     "geon_get_show_stars": (ctypes.c_int, []),
+    "geon_set_mixed_band": (ctypes.c_int, [ctypes.c_int, ctypes.c_double]),
+    "geon_get_mixed_band": (ctypes.c_double, [ctypes.c_int]),
+    "geon_set_mixed_reproject": (None, [ctypes.c_int]),
     "geon_riemann": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
     "geon_ricci": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
     "geon_ricci_scalar": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
@@ -93,6 +96,13 @@ SIGNATURES = {
     "geon_shadow_bisect": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_double_p, c_size_t,
                                           ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
                                           c_double_p, c_double_p, c_double_p, c_int64_p]),
+    "geon_shadow_classify_dev": (ctypes.c_int, [c_void_p, ctypes.c_double, c_void_p, c_size_t, ctypes.c_double,
+                                                ctypes.c_int64, ctypes.c_int, c_void_p, c_void_p, c_void_p]),
+    "geon_shadow_bisect_dev": (ctypes.c_int, [c_void_p, ctypes.c_double, c_void_p, c_void_p, c_size_t,
+                                              ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
+                                              c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "geon_launch_count": (ctypes.c_ulonglong, []),
+    "geon_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, c_double_p]),
 }
 
 _lib = None

@@ -24,6 +24,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
 # (source, extra flags)
 UNITS = [
     ("trace_fp64.cu", ["--fmad=false"]),
+    ("trace_mixed.cu", ["--fmad=false"]),
     ("curvature_fp64.cu", ["--fmad=false"]),
     ("capi.cu", ["--fmad=false"]),
 ]

@@ -24,6 +24,13 @@ namespace {
 
 thread_local std::string g_last_error;
 std::atomic<int> g_show_stars{1};
+// Mixed-precision options: FP64 band half-width per metric kind (in units of
+// M, b0, s; 0 disables) and the null re-projection switch.
+std::atomic<float> g_band[4] = {{0.0f}, {4.0f}, {3.0f}, {1.5f}};
+std::atomic<int> g_reproject{0};
+// Kernels launched by this library since load (ours only; memsets excluded).
+std::atomic<unsigned long long> g_launches{0};
+inline void counted(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -92,6 +99,7 @@ int make_camera(geon_metric_t m, const geon_camera* cam, int64_t spa, CameraDesc
   double* d_tet = d_obs + 4;
   int* d_status = reinterpret_cast<int*>(d_obs + 20);
   GEON_CUDA(cudaMemcpyAsync(d_obs, cam->observer, sizeof(double) * 4, cudaMemcpyHostToDevice, s));
+  counted();
   GEON_CUDA(launch_tetrad(m->desc, d_obs, d_tet, d_status, s));
   double tet[16];
   int status = 0;
@@ -124,8 +132,17 @@ TraceLaunch base_launch(geon_metric_t m, double step, int64_t max_steps) {
   L.half_step = 0.5 * step;
   L.sixth = step / 6.0;
   L.max_steps = max_steps;
+  L.band = g_band[m->desc.kind].load();
+  L.mixed_flags = g_reproject.load() ? MIXED_REPROJECT : 0;
   return L;
 }
+
+cudaError_t launch_trace(const TraceLaunch& L, int precision, int src, int sink, cudaStream_t s) {
+  if (L.n > 0) counted();
+  return precision == GEON_MIXED ? launch_trace_mixed(L, src, sink, s) : launch_trace_fp64(L, src, sink, s);
+}
+
+bool valid_precision(int p) { return p == GEON_FP64 || p == GEON_MIXED; }
 
 int copy_out(void* host, const void* dev, size_t bytes, cudaStream_t s) {
   if (host && bytes) GEON_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s));
@@ -161,6 +178,20 @@ void geon_render_config_default(geon_render_config* cfg) {
 }
 
 void geon_set_show_stars(int on) { g_show_stars.store(on ? 1 : 0); }
+
+int geon_set_mixed_band(int kind, double band) {
+  if (kind < GEON_MINKOWSKI || kind > GEON_MORRIS_THORNE || !(band >= 0.0))
+    return fail(GEON_ERR_INVALID, "bad band");
+  g_band[kind].store((float)band);
+  return GEON_OK;
+}
+
+double geon_get_mixed_band(int kind) {
+  if (kind < GEON_MINKOWSKI || kind > GEON_MORRIS_THORNE) return -1.0;
+  return (double)g_band[kind].load();
+}
+
+void geon_set_mixed_reproject(int on) { g_reproject.store(on ? 1 : 0); }
 int geon_get_show_stars(void) { return g_show_stars.load(); }
 
 int geon_metric_create(int kind, const double* params, int nparams, geon_metric_t* out) {
@@ -186,7 +217,8 @@ int geon_metric_create(int kind, const double* params, int nparams, geon_metric_
     DBuf b;
     GEON_CUDA(b.alloc(sizeof(MetricDesc), s));
     GEON_CUDA(cudaMemcpyAsync(b.p, &d, sizeof d, cudaMemcpyHostToDevice, s));
-    GEON_CUDA(launch_metric_init(b.as<MetricDesc>(), s));
+    counted();
+  GEON_CUDA(launch_metric_init(b.as<MetricDesc>(), s));
     GEON_CUDA(cudaMemcpyAsync(&d, b.p, sizeof d, cudaMemcpyDeviceToHost, s));
     GEON_CUDA(cudaStreamSynchronize(s));
   }
@@ -221,6 +253,7 @@ static int pointwise(geon_metric_t m, int what, const double* in, size_t n, int 
   GEON_CUDA(dflags.alloc(sizeof(int), s));
   GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
   GEON_CUDA(cudaMemcpyAsync(din.p, in, sizeof(double) * n * in_width, cudaMemcpyHostToDevice, s));
+  counted();
   GEON_CUDA(launch_pointwise(m->desc, what, din.as<double>(), (int64_t)n, out ? dout.as<double>() : nullptr,
                              out ? nullptr : dout.as<int32_t>(), dflags.as<int>(), s));
   if (out) GEON_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double) * n * out_width, cudaMemcpyDeviceToHost, s));
@@ -241,7 +274,7 @@ int geon_trace_dev(geon_metric_t m, const double* y0, size_t n, double step, int
                    int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual,
                    void* stream) {
   if (int rc = check_metric(m)) return rc;
-  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
   if (n == 0) return GEON_OK;
   if (!y0 || !term || !final_state || !steps_taken || !null_residual)
     return fail(GEON_ERR_INVALID, "geon_trace_dev needs every device buffer");
@@ -259,14 +292,14 @@ int geon_trace_dev(geon_metric_t m, const double* y0, size_t n, double step, int
   L.resid = null_residual;
   L.queue = ws.as<unsigned long long>();
   L.flags = reinterpret_cast<int*>(L.queue + 1);
-  GEON_CUDA(launch_trace_fp64(L, SRC_ARRAY, SINK_TRACE, s));
+  GEON_CUDA(launch_trace(L, precision, SRC_ARRAY, SINK_TRACE, s));
   return GEON_OK;
 }
 
 int geon_trace(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps, int precision,
                int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual) {
   if (int rc = check_metric(m)) return rc;
-  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
   if (n == 0) return GEON_OK;
   if (!y0 || !term) return fail(GEON_ERR_INVALID, "null buffer");
   if (max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
@@ -289,7 +322,7 @@ int geon_trace(geon_metric_t m, const double* y0, size_t n, double step, int64_t
   L.resid = dres.as<double>();
   L.queue = ws.as<unsigned long long>();
   L.flags = reinterpret_cast<int*>(L.queue + 1);
-  GEON_CUDA(launch_trace_fp64(L, SRC_ARRAY, SINK_TRACE, s));
+  GEON_CUDA(launch_trace(L, precision, SRC_ARRAY, SINK_TRACE, s));
   if (int rc = copy_out(term, dterm.p, sizeof(int32_t) * n, s)) return rc;
   if (int rc = copy_out(final_state, dyf.p, sizeof(double) * 8 * n, s)) return rc;
   if (int rc = copy_out(steps_taken, dsteps.p, sizeof(int64_t) * n, s)) return rc;
@@ -337,6 +370,7 @@ int geon_camera_ray_states(const geon_camera* cam, const double tetrad[16], doub
   cudaStream_t s = host_stream();
   DBuf d;
   GEON_CUDA(d.alloc(sizeof(double) * 8 * n, s));
+  counted();
   GEON_CUDA(launch_camera_rays(c, du, dv, d.as<double>(), s));
   GEON_CUDA(cudaMemcpyAsync(out_states, d.p, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s));
   GEON_CUDA(cudaStreamSynchronize(s));
@@ -347,7 +381,7 @@ int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_co
                    geon_render_stats* stats, int32_t* pixel_class, int64_t* pixel_steps) {
   if (int rc = check_metric(m)) return rc;
   if (!cfg || !rgb) return fail(GEON_ERR_INVALID, "null buffer");
-  if (cfg->precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (!valid_precision(cfg->precision)) return fail(GEON_ERR_INVALID, "unknown precision");
   if (cfg->max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
   cudaStream_t s = host_stream();
   const int64_t spa = cfg->samples_per_axis < 1 ? 1 : cfg->samples_per_axis;
@@ -382,7 +416,8 @@ int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_co
   L.queue = wsu;
   L.flags = reinterpret_cast<int*>(wsu + 1);
   unsigned long long* dstats = wsu + 2;  // 6 counters
-  GEON_CUDA(launch_trace_fp64(L, SRC_CAMERA, SINK_RENDER, s));
+  GEON_CUDA(launch_trace(L, cfg->precision, SRC_CAMERA, SINK_RENDER, s));
+  counted();
   GEON_CUDA(launch_render_reduce(dsrgb.as<float>(), dterm.as<int32_t>(), dsteps.as<int64_t>(),
                                  dres.as<double>(), npix, spa, drgb.as<float>(), dcls.as<int32_t>(),
                                  dpst.as<int64_t>(), dstats, s));
@@ -419,6 +454,7 @@ int geon_sky_sample(const double* dir, size_t n, int show_stars, float* rgb) {
   GEON_CUDA(dd.alloc(sizeof(double) * 3 * n, s));
   GEON_CUDA(dr.alloc(sizeof(float) * 3 * n, s));
   GEON_CUDA(cudaMemcpyAsync(dd.p, dir, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  counted();
   GEON_CUDA(launch_sky(dd.as<double>(), (int64_t)n, show_stars, dr.as<float>(), s));
   GEON_CUDA(cudaMemcpyAsync(rgb, dr.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s));
   GEON_CUDA(cudaStreamSynchronize(s));
@@ -440,6 +476,7 @@ static int curvature_call(geon_metric_t m, int what, const double* x, size_t n, 
   GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
   GEON_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, s));
   if (kcount) GEON_CUDA(cudaMemcpyAsync(dk.p, k, sizeof(double) * 4 * kcount, cudaMemcpyHostToDevice, s));
+  counted();
   GEON_CUDA(launch_curvature(m->desc, what, dx.as<double>(), (int64_t)n, dk.as<double>(), (int64_t)nk,
                              k_shared, dout.as<double>(), dflags.as<int>(), s));
   GEON_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double) * n * out_width, cudaMemcpyDeviceToHost, s));
@@ -476,6 +513,7 @@ int geon_equatorial_rays(geon_metric_t m, double r_obs, const double* alpha, siz
   GEON_CUDA(da.alloc(sizeof(double) * n, s));
   GEON_CUDA(dout.alloc(sizeof(double) * 8 * n, s));
   GEON_CUDA(cudaMemcpyAsync(da.p, alpha, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  counted();
   GEON_CUDA(launch_equatorial_rays(m->desc.p[0], r_obs, da.as<double>(), (int64_t)n, dout.as<double>(), s));
   GEON_CUDA(cudaMemcpyAsync(out_states, dout.p, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s));
   GEON_CUDA(cudaStreamSynchronize(s));
@@ -484,7 +522,8 @@ int geon_equatorial_rays(geon_metric_t m, double r_obs, const double* alpha, siz
 
 // Classify rays launched at the given angles on stream s (device buffers).
 static int classify_dev(geon_metric_t m, double r_obs, const double* d_alpha, int64_t n, double step,
-                        int64_t max_steps, int32_t* d_term, int64_t* d_steps, cudaStream_t s) {
+                        int64_t max_steps, int precision, int32_t* d_term, int64_t* d_steps,
+                        cudaStream_t s) {
   DBuf ws;
   GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 2, s));
   GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 2, s));
@@ -496,7 +535,7 @@ static int classify_dev(geon_metric_t m, double r_obs, const double* d_alpha, in
   L.steps = d_steps;
   L.queue = ws.as<unsigned long long>();
   L.flags = reinterpret_cast<int*>(L.queue + 1);
-  GEON_CUDA(launch_trace_fp64(L, SRC_EQUATORIAL, SINK_SHADOW, s));
+  GEON_CUDA(launch_trace(L, precision, SRC_EQUATORIAL, SINK_SHADOW, s));
   return GEON_OK;
 }
 
@@ -504,7 +543,7 @@ int geon_shadow_classify(geon_metric_t m, double r_obs, const double* alpha, siz
                          int64_t max_steps, int precision, int32_t* term, int64_t* steps) {
   if (int rc = check_metric(m)) return rc;
   if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow classification needs a Schwarzschild metric");
-  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
   if (n == 0) return GEON_OK;
   if (!alpha || !term) return fail(GEON_ERR_INVALID, "null buffer");
   cudaStream_t s = host_stream();
@@ -513,8 +552,8 @@ int geon_shadow_classify(geon_metric_t m, double r_obs, const double* alpha, siz
   GEON_CUDA(dt.alloc(sizeof(int32_t) * n, s));
   GEON_CUDA(dst.alloc(sizeof(int64_t) * n, s));
   GEON_CUDA(cudaMemcpyAsync(da.p, alpha, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  if (int rc = classify_dev(m, r_obs, da.as<double>(), (int64_t)n, step, max_steps, dt.as<int32_t>(),
-                            dst.as<int64_t>(), s))
+  if (int rc = classify_dev(m, r_obs, da.as<double>(), (int64_t)n, step, max_steps, precision,
+                            dt.as<int32_t>(), dst.as<int64_t>(), s))
     return rc;
   GEON_CUDA(cudaMemcpyAsync(term, dt.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
   if (int rc = copy_out(steps, dst.p, sizeof(int64_t) * n, s)) return rc;
@@ -524,87 +563,140 @@ int geon_shadow_classify(geon_metric_t m, double r_obs, const double* alpha, siz
 
 // Bisection of bin/validate_shadow.rs:70-79, evaluated L levels at a time: for
 // each bracket every midpoint the next L sequential halvings could visit (a
-// complete binary tree of 2^L - 1 launch angles, built with the same
-// 0.5*(lo+hi) arithmetic) is traced in one launch, then the sequential path is
-// replayed through the tree. The result equals the sequential loop bit for
-// bit, with ceil(iters / L) dependent launches instead of iters.
+// complete binary tree of 2^L - 1 launch angles, built on the device with the
+// same 0.5*(lo+hi) arithmetic) is traced in one launch, then a walk kernel
+// replays the sequential path through the tree. The result equals the
+// sequential loop bit for bit, with ceil(iters / L) dependent rounds instead of
+// iters, and no host round trip between rounds (3 launches per round).
+static int64_t bisect_levels(size_t nb) {
+  const int64_t target_rays = 16384;
+  int L = 1;
+  while (L < 16 && (int64_t)nb * ((1LL << (L + 1)) - 1) <= target_rays) ++L;
+  return L;
+}
+
+int geon_shadow_bisect_dev(geon_metric_t m, double r_obs, const double* lo, const double* hi, size_t nb,
+                           int iters, double step, int64_t max_steps, int precision, double* alpha_c,
+                           double* lo_out, double* hi_out, int64_t* steps_out, void* stream) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow bisection needs a Schwarzschild metric");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (nb == 0) return GEON_OK;
+  if (!lo || !hi || !alpha_c || iters < 0 || max_steps < 0) return fail(GEON_ERR_INVALID, "bad bisection arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int Lmax = (int)bisect_levels(nb);
+  const int64_t cap = (int64_t)nb * ((1LL << Lmax) - 1);
+  DBuf work, tree, tterm, tsteps, ws;
+  GEON_CUDA(work.alloc(sizeof(double) * 2 * nb + sizeof(int64_t) * nb, s));
+  GEON_CUDA(tree.alloc(sizeof(double) * cap, s));
+  GEON_CUDA(tterm.alloc(sizeof(int32_t) * cap, s));
+  GEON_CUDA(tsteps.alloc(sizeof(int64_t) * cap, s));
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 2, s));
+  double* wlo = work.as<double>();
+  double* whi = wlo + nb;
+  int64_t* wst = reinterpret_cast<int64_t*>(whi + nb);
+  GEON_CUDA(cudaMemcpyAsync(wlo, lo, sizeof(double) * nb, cudaMemcpyDefault, s));
+  GEON_CUDA(cudaMemcpyAsync(whi, hi, sizeof(double) * nb, cudaMemcpyDefault, s));
+  GEON_CUDA(cudaMemsetAsync(wst, 0, sizeof(int64_t) * nb, s));
+  int remaining = iters;
+  while (remaining > 0) {
+    const int L = remaining < Lmax ? remaining : Lmax;
+    const int64_t per = (1LL << L) - 1;
+    const int64_t nr = (int64_t)nb * per;
+    counted();
+    GEON_CUDA(launch_bisect_build((int64_t)nb, per, wlo, whi, tree.as<double>(), s));
+    GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 2, s));
+    TraceLaunch T = base_launch(m, step, max_steps);
+    T.n = nr;
+    T.alpha = tree.as<double>();
+    T.r_obs = r_obs;
+    T.term = tterm.as<int32_t>();
+    T.steps = tsteps.as<int64_t>();
+    T.queue = ws.as<unsigned long long>();
+    T.flags = reinterpret_cast<int*>(T.queue + 1);
+    GEON_CUDA(launch_trace(T, precision, SRC_EQUATORIAL, SINK_SHADOW, s));
+    counted();
+    GEON_CUDA(launch_bisect_walk((int64_t)nb, per, L, tree.as<double>(), tterm.as<int32_t>(),
+                                 tsteps.as<int64_t>(), wlo, whi, wst, s));
+    remaining -= L;
+  }
+  counted();
+  GEON_CUDA(launch_bisect_finish((int64_t)nb, wlo, whi, alpha_c, s));
+  if (lo_out) GEON_CUDA(cudaMemcpyAsync(lo_out, wlo, sizeof(double) * nb, cudaMemcpyDefault, s));
+  if (hi_out) GEON_CUDA(cudaMemcpyAsync(hi_out, whi, sizeof(double) * nb, cudaMemcpyDefault, s));
+  if (steps_out) GEON_CUDA(cudaMemcpyAsync(steps_out, wst, sizeof(int64_t) * nb, cudaMemcpyDefault, s));
+  return GEON_OK;
+}
+
 int geon_shadow_bisect(geon_metric_t m, double r_obs, const double* lo, const double* hi, size_t nb, int iters,
                        double step, int64_t max_steps, int precision, double* alpha_c, double* lo_out,
                        double* hi_out, int64_t* steps_out) {
   if (int rc = check_metric(m)) return rc;
-  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow bisection needs a Schwarzschild metric");
-  if (precision != GEON_FP64) return fail(GEON_ERR_UNSUPPORTED, "precision not available for this call");
   if (nb == 0) return GEON_OK;
-  if (!lo || !hi || !alpha_c || iters < 0) return fail(GEON_ERR_INVALID, "bad bisection arguments");
-  std::vector<double> vlo(lo, lo + nb), vhi(hi, hi + nb);
-  std::vector<int64_t> vsteps(nb, 0);
-  const int64_t target_rays = 16384;
-  int Lmax = 1;
-  while (Lmax < 16 && (int64_t)nb * ((1LL << (Lmax + 1)) - 1) <= target_rays) ++Lmax;
+  if (!lo || !hi || !alpha_c) return fail(GEON_ERR_INVALID, "bad bisection arguments");
   cudaStream_t s = host_stream();
-  int remaining = iters;
-  const int64_t cap = (int64_t)nb * ((1LL << Lmax) - 1);
-  DBuf da, dt, dst;
-  GEON_CUDA(da.alloc(sizeof(double) * cap, s));
-  GEON_CUDA(dt.alloc(sizeof(int32_t) * cap, s));
-  GEON_CUDA(dst.alloc(sizeof(int64_t) * cap, s));
-  std::vector<double> alpha(cap), node_lo(cap), node_hi(cap);
-  std::vector<int32_t> term(cap);
-  std::vector<int64_t> st(cap);
-  while (remaining > 0) {
-    const int L = remaining < Lmax ? remaining : Lmax;
-    const int64_t per = (1LL << L) - 1;
-    // heap-ordered tree per bracket: node 1 is the root, children 2i / 2i+1
-    for (size_t b = 0; b < nb; ++b) {
-      double* a = &alpha[b * per];
-      double* nl = &node_lo[b * per];
-      double* nh = &node_hi[b * per];
-      nl[0] = vlo[b];
-      nh[0] = vhi[b];
-      for (int64_t i = 1; i <= per; ++i) {
-        const double l = nl[i - 1], h = nh[i - 1];
-        const double mid = 0.5 * (l + h);
-        a[i - 1] = mid;
-        if (2 * i <= per) {  // left child: not captured -> hi = mid
-          nl[2 * i - 1] = l;
-          nh[2 * i - 1] = mid;
-        }
-        if (2 * i + 1 <= per) {  // right child: captured -> lo = mid
-          nl[2 * i] = mid;
-          nh[2 * i] = h;
-        }
-      }
-    }
-    const int64_t nr = (int64_t)nb * per;
-    GEON_CUDA(cudaMemcpyAsync(da.p, alpha.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, s));
-    if (int rc = classify_dev(m, r_obs, da.as<double>(), nr, step, max_steps, dt.as<int32_t>(),
-                              dst.as<int64_t>(), s))
-      return rc;
-    GEON_CUDA(cudaMemcpyAsync(term.data(), dt.p, sizeof(int32_t) * nr, cudaMemcpyDeviceToHost, s));
-    GEON_CUDA(cudaMemcpyAsync(st.data(), dst.p, sizeof(int64_t) * nr, cudaMemcpyDeviceToHost, s));
-    GEON_CUDA(cudaStreamSynchronize(s));
-    for (size_t b = 0; b < nb; ++b) {
-      int64_t node = 1;
-      for (int d = 0; d < L; ++d) {
-        const double mid = alpha[b * per + node - 1];
-        vsteps[b] += st[b * per + node - 1];
-        if (term[b * per + node - 1] == TERM_CAPTURED) {
-          vlo[b] = mid;
-          node = 2 * node + 1;
-        } else {
-          vhi[b] = mid;
-          node = 2 * node;
-        }
-      }
-    }
-    remaining -= L;
+  DBuf io;
+  GEON_CUDA(io.alloc(sizeof(double) * 5 * nb + sizeof(int64_t) * nb, s));
+  double* d_lo = io.as<double>();
+  double* d_hi = d_lo + nb;
+  double* d_ac = d_hi + nb;
+  double* d_lo_o = d_ac + nb;
+  double* d_hi_o = d_lo_o + nb;
+  int64_t* d_st = reinterpret_cast<int64_t*>(d_hi_o + nb);
+  GEON_CUDA(cudaMemcpyAsync(d_lo, lo, sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(cudaMemcpyAsync(d_hi, hi, sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+  if (int rc = geon_shadow_bisect_dev(m, r_obs, d_lo, d_hi, nb, iters, step, max_steps, precision, d_ac, d_lo_o,
+                                      d_hi_o, d_st, s))
+    return rc;
+  GEON_CUDA(cudaMemcpyAsync(alpha_c, d_ac, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
+  if (int rc = copy_out(lo_out, d_lo_o, sizeof(double) * nb, s)) return rc;
+  if (int rc = copy_out(hi_out, d_hi_o, sizeof(double) * nb, s)) return rc;
+  if (int rc = copy_out(steps_out, d_st, sizeof(int64_t) * nb, s)) return rc;
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+int geon_shadow_classify_dev(geon_metric_t m, double r_obs, const double* alpha, size_t n, double step,
+                             int64_t max_steps, int precision, int32_t* term, int64_t* steps, void* stream) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow classification needs a Schwarzschild metric");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (n == 0) return GEON_OK;
+  if (!alpha || !term) return fail(GEON_ERR_INVALID, "null buffer");
+  return classify_dev(m, r_obs, alpha, (int64_t)n, step, max_steps, precision, term, steps,
+                      static_cast<cudaStream_t>(stream));
+}
+
+unsigned long long geon_launch_count(void) { return g_launches.load(); }
+
+int geon_probe_fma_peak(int fp64, double* tflops) {
+  if (!tflops) return fail(GEON_ERR_INVALID, "null output");
+  int dev = 0, sms = 0;
+  GEON_CUDA(cudaGetDevice(&dev));
+  GEON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256;
+  const int iters = fp64 ? 4096 : 65536;
+  cudaStream_t s = host_stream();
+  DBuf out;
+  GEON_CUDA(out.alloc((size_t)blocks * threads * 8, s));
+  cudaEvent_t a, b;
+  GEON_CUDA(cudaEventCreate(&a));
+  GEON_CUDA(cudaEventCreate(&b));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    GEON_CUDA(cudaEventRecord(a, s));
+    counted();
+    GEON_CUDA(launch_fma_probe(fp64, out.p, blocks, threads, iters, s));
+    GEON_CUDA(cudaEventRecord(b, s));
+    GEON_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    GEON_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (rep > 0 && ms < best) best = ms;
   }
-  for (size_t b = 0; b < nb; ++b) {
-    alpha_c[b] = 0.5 * (vlo[b] + vhi[b]);
-    if (lo_out) lo_out[b] = vlo[b];
-    if (hi_out) hi_out[b] = vhi[b];
-    if (steps_out) steps_out[b] = vsteps[b];
-  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+  *tflops = flops / (best * 1e-3) / 1e12;
   return GEON_OK;
 }
 

@@ -36,6 +36,8 @@ struct CameraDesc {
   int forward_sign;
 };
 
+enum : int { MIXED_REPROJECT = 1 };
+
 // Sources of initial states.
 enum : int { SRC_ARRAY = 0, SRC_CAMERA = 1, SRC_EQUATORIAL = 2 };
 // Where results go.
@@ -64,6 +66,9 @@ struct TraceLaunch {
   int show_stars;
   float captured_rgb[3];  // RenderConfig::captured_rgb (render.rs:20)
   float diverged_rgb[3];  // RenderConfig::diverged_rgb (render.rs:25)
+  // mixed precision
+  float band;          // FP64 band half-width in the metric's own scale (0 = no band)
+  int mixed_flags;     // MIXED_* bits
   // work queue
   unsigned long long* queue;  // next unclaimed ray index
   int* flags;                 // bit 0: a metric became singular (inverse of g failed)
@@ -71,6 +76,8 @@ struct TraceLaunch {
 
 // ---- launchers (trace_fp64.cu) ----
 cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStream_t s);
+// ---- launchers (trace_mixed.cu) ----
+cudaError_t launch_trace_mixed(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,
                                  const double* resid, int64_t npix, int64_t spa, float* rgb,
                                  int32_t* pclass, int64_t* psteps, unsigned long long* stats,
@@ -81,7 +88,14 @@ cudaError_t launch_tetrad(const MetricDesc& M, const double* obs, double* out16,
                           cudaStream_t s);
 cudaError_t launch_metric_init(MetricDesc* d_desc, cudaStream_t s);
 cudaError_t launch_sky(const double* dir, int64_t n, int show, float* rgb, cudaStream_t s);
-int trace_fp64_blocks_per_sm(int kind, int src, int sink);
+cudaError_t launch_bisect_build(int64_t nb, int64_t per, const double* lo, const double* hi, double* alpha,
+                                cudaStream_t s);
+cudaError_t launch_bisect_walk(int64_t nb, int64_t per, int levels, const double* alpha, const int32_t* term,
+                               const int64_t* steps, double* lo, double* hi, int64_t* path_steps,
+                               cudaStream_t s);
+cudaError_t launch_bisect_finish(int64_t nb, const double* lo, const double* hi, double* alpha_c,
+                                 cudaStream_t s);
+cudaError_t launch_fma_probe(int fp64, void* out, int blocks, int threads, int iters, cudaStream_t s);
 
 // ---- launchers (curvature_fp64.cu) ----
 // what: 0 riemann, 1 ricci, 2 ricci_scalar, 3 einstein, 4 stress_energy, 5 nec

@@ -1,0 +1,170 @@
+// Ray sources, result sinks and the persistent work-queue loop shared by the
+// FP64 and mixed-precision steppers.
+//
+// One thread owns one ray at a time; the ray state stays in registers for its
+// whole life. Each warp pulls ray indices from a device work queue with one
+// atomic per refill (ballot + popc + shuffle), so a lane whose ray is captured
+// or escapes picks up a fresh ray at the next step instead of idling until the
+// slowest ray of its warp finishes.
+#pragma once
+#include "internal.h"
+#include "metric_fp64.cuh"
+#include "sky.cuh"
+
+namespace geon {
+
+// ---------------------------------------------------------------------------
+// Sources of initial states
+// ---------------------------------------------------------------------------
+// camera.rs:113-160 (ray_state_sub), with forward_sign = +1 the reference.
+__device__ __forceinline__ void camera_ray(const CameraDesc& c, int64_t ray, double y[8]) {
+  const int64_t spa2 = c.spa * c.spa;
+  const int64_t pix = ray / spa2;
+  const int64_t sub = ray - pix * spa2;
+  const int64_t sj = sub / c.spa, si = sub - sj * c.spa;
+  const int64_t j = pix / c.width, i = pix - j * c.width;
+  const double du = ((double)si + 0.5) * c.inv_spa;
+  const double dv = ((double)sj + 0.5) * c.inv_spa;
+  const double u = (2.0 * ((double)i + du) / c.width_d - 1.0) * c.w_img;
+  const double v = -(2.0 * ((double)j + dv) / c.height_d - 1.0) * c.h_img;
+  const double fs = (double)c.forward_sign;
+  const double dx = -fs;
+  const double dy = -v;
+  const double dz = c.forward_sign == 1 ? u : fs * u;
+  const double norm = sqrt(dx * dx + dy * dy + dz * dz);
+  const double n1 = dx / norm, n2 = dy / norm, n3 = dz / norm;
+#pragma unroll
+  for (int mu = 0; mu < 4; ++mu) y[mu] = c.obs[mu];
+#pragma unroll
+  for (int mu = 0; mu < 4; ++mu)
+    y[4 + mu] = c.tet[0][mu] + n1 * c.tet[1][mu] + n2 * c.tet[2][mu] + n3 * c.tet[3][mu];
+}
+
+// bin/validate_shadow.rs:20-35
+__device__ __forceinline__ void equatorial_ray(double m, double r_obs, double alpha, double y[8]) {
+  const double f = 1.0 - 2.0 * m / r_obs;
+  double sin_a, cos_a;
+  dm::sincos_det(alpha, &sin_a, &cos_a);
+  const double sf = sqrt(f);
+  y[0] = 0.0;
+  y[1] = r_obs;
+  y[2] = 1.5707963267948966;  // FRAC_PI_2
+  y[3] = 0.0;
+  y[4] = 1.0 / sf;
+  y[5] = -cos_a * sf;
+  y[6] = 0.0;
+  y[7] = sin_a / r_obs;
+}
+
+template <int SRC>
+__device__ __forceinline__ void load_ray(const TraceLaunch& L, int64_t ray, double y[8]) {
+  if (SRC == SRC_ARRAY) {
+    const double2* p = reinterpret_cast<const double2*>(L.y0 + 8 * ray);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double2 v = p[q];
+      y[2 * q] = v.x;
+      y[2 * q + 1] = v.y;
+    }
+  } else if (SRC == SRC_CAMERA) {
+    camera_ray(L.cam, ray, y);
+  } else {
+    equatorial_ray(L.M.p[0], L.r_obs, L.alpha[ray], y);
+  }
+}
+
+template <int K, int SINK>
+__device__ __forceinline__ void store_ray(const TraceLaunch& L, int64_t ray, int term,
+                                          const double y[8], int64_t steps) {
+  if (SINK == SINK_SHADOW) {
+    L.term[ray] = term;
+    if (L.steps) L.steps[ray] = steps;
+    return;
+  }
+  const double resid = null_residual<K>(L.M, y);
+  if (SINK == SINK_TRACE) {
+    L.term[ray] = term;
+    double2* o = reinterpret_cast<double2*>(L.yfinal + 8 * ray);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_double2(y[2 * q], y[2 * q + 1]);
+    L.steps[ray] = steps;
+    L.resid[ray] = resid;
+  } else {  // SINK_RENDER (render.rs:77-101)
+    float rgb[3];
+    if (term == TERM_CAPTURED) {
+      rgb[0] = L.captured_rgb[0]; rgb[1] = L.captured_rgb[1]; rgb[2] = L.captured_rgb[2];
+    } else if (term == TERM_DIVERGED) {
+      rgb[0] = L.diverged_rgb[0]; rgb[1] = L.diverged_rgb[1]; rgb[2] = L.diverged_rgb[2];
+    } else {
+      double dir[3];
+      metric_asymptotic_direction<K>(y, y + 4, dir);
+      sky_sample(dir, L.show_stars != 0, rgb);
+    }
+    L.srgb[3 * ray + 0] = rgb[0];
+    L.srgb[3 * ray + 1] = rgb[1];
+    L.srgb[3 * ray + 2] = rgb[2];
+    L.term[ray] = term;
+    L.steps[ray] = steps;
+    L.resid[ray] = resid;
+  }
+}
+
+constexpr int TRACE_BLOCK = 128;
+
+// geodesic.rs:62-117 for every ray of the job, persistent over a work queue.
+// Stepper owns the ray state: load(y0), to_double(y), terminate(L), step(L)
+// (true = advanced, false = the new state was not finite; state unchanged).
+template <class Stepper, int K, int SRC, int SINK>
+__device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int64_t ray = -1;
+  int64_t n = 0;
+  Stepper st;
+  bool queue_open = true;
+  for (;;) {
+    const unsigned need = __ballot_sync(FULL, ray < 0);
+    if (need && queue_open) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(L.queue, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (base + __popc(need) >= (unsigned long long)L.n) queue_open = false;
+      if (ray < 0) {
+        const unsigned long long idx = base + __popc(need & lt_mask);
+        if (idx < (unsigned long long)L.n) {
+          ray = (int64_t)idx;
+          n = 0;
+          double y0[8];
+          load_ray<SRC>(L, ray, y0);
+          st.load(L, y0);
+        }
+      }
+    }
+    if (__ballot_sync(FULL, ray >= 0) == 0) break;
+    if (ray >= 0) {
+      int t = TERM_NONE;
+      int64_t taken = n;
+      if (n >= L.max_steps) {  // loop exhausted: Diverged with steps_taken = max_steps
+        t = TERM_DIVERGED;
+        taken = L.max_steps;
+      } else {
+        t = st.terminate(L);
+        if (t == TERM_NONE) {
+          if (st.step(L)) ++n;
+          else t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
+        }
+      }
+      if (t != TERM_NONE) {
+        double y[8];
+        st.to_double(y);
+        store_ray<K, SINK>(L, ray, t, y, taken);
+        ray = -1;
+      }
+    }
+  }
+  st.finish(L);
+}
+
+}  // namespace geon

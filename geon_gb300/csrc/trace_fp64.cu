@@ -1,176 +1,51 @@
-// FP64 parity path: persistent ray-tracing kernel and its helpers.
-//
-// One thread owns one ray at a time; the ray state (8 doubles) stays in
-// registers for its whole life. Each warp pulls ray indices from a device work
-// queue with one atomic per refill (ballot + popc + shuffle), so a lane whose
-// ray is captured or escapes picks up a fresh ray at the next step instead of
-// idling until the slowest ray of its warp finishes.
+// FP64 parity path: the persistent ray-tracing kernel (loop in
+// trace_common.cuh) with the reference's FP64 RK4 step, plus render reduction,
+// point-wise functors, tetrad, camera/equatorial ray generation and sky kernels.
 //
 // Compiled with --fmad=false: every FP64 result must match the CPU oracle.
 #include <cuda_runtime.h>
 
 #include "internal.h"
 #include "metric_fp64.cuh"
-#include "sky.cuh"
+#include "trace_common.cuh"
 
 namespace geon {
 
 // ---------------------------------------------------------------------------
-// Sources of initial states
+// FP64 stepper: the reference's arithmetic, bit for bit.
 // ---------------------------------------------------------------------------
-// camera.rs:113-160 (ray_state_sub), with forward_sign = +1 the reference.
-__device__ __forceinline__ void camera_ray(const CameraDesc& c, int64_t ray, double y[8]) {
-  const int64_t spa2 = c.spa * c.spa;
-  const int64_t pix = ray / spa2;
-  const int64_t sub = ray - pix * spa2;
-  const int64_t sj = sub / c.spa, si = sub - sj * c.spa;
-  const int64_t j = pix / c.width, i = pix - j * c.width;
-  const double du = ((double)si + 0.5) * c.inv_spa;
-  const double dv = ((double)sj + 0.5) * c.inv_spa;
-  const double u = (2.0 * ((double)i + du) / c.width_d - 1.0) * c.w_img;
-  const double v = -(2.0 * ((double)j + dv) / c.height_d - 1.0) * c.h_img;
-  const double fs = (double)c.forward_sign;
-  const double dx = -fs;
-  const double dy = -v;
-  const double dz = c.forward_sign == 1 ? u : fs * u;
-  const double norm = sqrt(dx * dx + dy * dy + dz * dz);
-  const double n1 = dx / norm, n2 = dy / norm, n3 = dz / norm;
+template <int K>
+struct Fp64Stepper {
+  double y[8];
+  bool singular = false;
+  __device__ __forceinline__ void load(const TraceLaunch&, const double y0[8]) {
 #pragma unroll
-  for (int mu = 0; mu < 4; ++mu) y[mu] = c.obs[mu];
-#pragma unroll
-  for (int mu = 0; mu < 4; ++mu)
-    y[4 + mu] = c.tet[0][mu] + n1 * c.tet[1][mu] + n2 * c.tet[2][mu] + n3 * c.tet[3][mu];
-}
-
-// bin/validate_shadow.rs:20-35
-__device__ __forceinline__ void equatorial_ray(double m, double r_obs, double alpha, double y[8]) {
-  const double f = 1.0 - 2.0 * m / r_obs;
-  double sin_a, cos_a;
-  dm::sincos_det(alpha, &sin_a, &cos_a);
-  const double sf = sqrt(f);
-  y[0] = 0.0;
-  y[1] = r_obs;
-  y[2] = 1.5707963267948966;  // FRAC_PI_2
-  y[3] = 0.0;
-  y[4] = 1.0 / sf;
-  y[5] = -cos_a * sf;
-  y[6] = 0.0;
-  y[7] = sin_a / r_obs;
-}
-
-template <int SRC>
-__device__ __forceinline__ void load_ray(const TraceLaunch& L, int64_t ray, double y[8]) {
-  if (SRC == SRC_ARRAY) {
-    const double2* p = reinterpret_cast<const double2*>(L.y0 + 8 * ray);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const double2 v = p[q];
-      y[2 * q] = v.x;
-      y[2 * q + 1] = v.y;
-    }
-  } else if (SRC == SRC_CAMERA) {
-    camera_ray(L.cam, ray, y);
-  } else {
-    equatorial_ray(L.M.p[0], L.r_obs, L.alpha[ray], y);
+    for (int i = 0; i < 8; ++i) y[i] = y0[i];
   }
-}
-
-template <int K, int SINK>
-__device__ __forceinline__ void store_ray(const TraceLaunch& L, int64_t ray, int term,
-                                          const double y[8], int64_t steps) {
-  if (SINK == SINK_SHADOW) {
-    L.term[ray] = term;
-    if (L.steps) L.steps[ray] = steps;
-    return;
-  }
-  const double resid = null_residual<K>(L.M, y);
-  if (SINK == SINK_TRACE) {
-    L.term[ray] = term;
-    double2* o = reinterpret_cast<double2*>(L.yfinal + 8 * ray);
+  __device__ __forceinline__ void to_double(double out[8]) const {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) o[q] = make_double2(y[2 * q], y[2 * q + 1]);
-    L.steps[ray] = steps;
-    L.resid[ray] = resid;
-  } else {  // SINK_RENDER (render.rs:77-101)
-    float rgb[3];
-    if (term == TERM_CAPTURED) {
-      rgb[0] = L.captured_rgb[0]; rgb[1] = L.captured_rgb[1]; rgb[2] = L.captured_rgb[2];
-    } else if (term == TERM_DIVERGED) {
-      rgb[0] = L.diverged_rgb[0]; rgb[1] = L.diverged_rgb[1]; rgb[2] = L.diverged_rgb[2];
-    } else {
-      double dir[3];
-      metric_asymptotic_direction<K>(y, y + 4, dir);
-      sky_sample(dir, L.show_stars != 0, rgb);
-    }
-    L.srgb[3 * ray + 0] = rgb[0];
-    L.srgb[3 * ray + 1] = rgb[1];
-    L.srgb[3 * ray + 2] = rgb[2];
-    L.term[ray] = term;
-    L.steps[ray] = steps;
-    L.resid[ray] = resid;
+    for (int i = 0; i < 8; ++i) out[i] = y[i];
   }
-}
+  __device__ __forceinline__ int terminate(const TraceLaunch& L) const { return metric_terminate<K>(L.M, y); }
+  __device__ __forceinline__ bool step(const TraceLaunch& L) {
+    double yn[8];
+    singular |= !rk4_step<K>(L.M, y, L.step, L.half_step, L.sixth, yn);
+    bool finite = true;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) finite &= isfinite(yn[i]);
+    if (!finite) return false;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = yn[i];
+    return true;
+  }
+  __device__ __forceinline__ void finish(const TraceLaunch& L) {
+    if (singular) atomicOr(L.flags, 1);
+  }
+};
 
-constexpr int TRACE_BLOCK = 128;
-
-// geodesic.rs:62-117 for every ray of the job, persistent over a work queue.
 template <int K, int SRC, int SINK>
 __global__ void __launch_bounds__(TRACE_BLOCK) trace_fp64_kernel(const TraceLaunch L) {
-  const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const unsigned lt_mask = (1u << lane) - 1u;
-  int64_t ray = -1;
-  int64_t n = 0;
-  double y[8];
-  bool queue_open = true;
-  bool singular = false;
-  for (;;) {
-    // Refill idle lanes from the queue (one atomic per warp).
-    const unsigned need = __ballot_sync(FULL, ray < 0);
-    if (need && queue_open) {
-      const int leader = __ffs(need) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(L.queue, (unsigned long long)__popc(need));
-      base = __shfl_sync(FULL, base, leader);
-      if (base + __popc(need) >= (unsigned long long)L.n) queue_open = false;
-      if (ray < 0) {
-        const unsigned long long idx = base + __popc(need & lt_mask);
-        if (idx < (unsigned long long)L.n) {
-          ray = (int64_t)idx;
-          n = 0;
-          load_ray<SRC>(L, ray, y);
-        }
-      }
-    }
-    if (__ballot_sync(FULL, ray >= 0) == 0) break;
-    if (ray >= 0) {
-      if (n >= L.max_steps) {  // loop exhausted: Diverged with steps_taken = max_steps
-        store_ray<K, SINK>(L, ray, TERM_DIVERGED, y, L.max_steps);
-        ray = -1;
-      } else {
-        const int t = metric_terminate<K>(L.M, y);
-        if (t != TERM_NONE) {
-          store_ray<K, SINK>(L, ray, t, y, n);
-          ray = -1;
-        } else {
-          double yn[8];
-          singular |= !rk4_step<K>(L.M, y, L.step, L.half_step, L.sixth, yn);
-          bool finite = true;
-#pragma unroll
-          for (int i = 0; i < 8; ++i) finite &= isfinite(yn[i]);
-          if (!finite) {
-            store_ray<K, SINK>(L, ray, TERM_DIVERGED, y, n);
-            ray = -1;
-          } else {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) y[i] = yn[i];
-            ++n;
-          }
-        }
-      }
-    }
-  }
-  if (singular) atomicOr(L.flags, 1);
+  trace_loop<Fp64Stepper<K>, K, SRC, SINK>(L);
 }
 
 template <int K, int SRC, int SINK>
@@ -459,6 +334,99 @@ cudaError_t launch_equatorial_rays(double m, double r_obs, const double* alpha, 
                                    cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   equatorial_rays_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(m, r_obs, alpha, n, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Device-side bisection rounds (bin/validate_shadow.rs:70-79, L levels per round)
+// ---------------------------------------------------------------------------
+// alpha[b*per + i-1] = midpoint of heap node i (1-based) of bracket b: the
+// interval of node i follows from the bits of i below its leading one (1 =
+// captured: lo = mid; 0 = escaped or diverged: hi = mid), with the same
+// 0.5*(lo+hi) arithmetic as the sequential loop.
+__global__ void bisect_build_kernel(int64_t nb, int64_t per, const double* __restrict__ lo,
+                                    const double* __restrict__ hi, double* __restrict__ alpha) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nb * per) return;
+  const int64_t b = t / per;
+  const int64_t node = t - b * per + 1;
+  double l = lo[b], h = hi[b];
+  int depth = 63 - __clzll((long long)node);
+  for (int d = depth - 1; d >= 0; --d) {
+    const double mid = 0.5 * (l + h);
+    if ((node >> d) & 1) l = mid;
+    else h = mid;
+  }
+  alpha[t] = 0.5 * (l + h);
+}
+
+__global__ void bisect_walk_kernel(int64_t nb, int64_t per, int levels, const double* __restrict__ alpha,
+                                   const int32_t* __restrict__ term, const int64_t* __restrict__ steps,
+                                   double* __restrict__ lo, double* __restrict__ hi,
+                                   int64_t* __restrict__ path_steps) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  int64_t node = 1;
+  double l = lo[b], h = hi[b];
+  int64_t acc = path_steps ? path_steps[b] : 0;
+  for (int d = 0; d < levels; ++d) {
+    const int64_t q = b * per + node - 1;
+    acc += steps[q];
+    if (term[q] == TERM_CAPTURED) {
+      l = alpha[q];
+      node = 2 * node + 1;
+    } else {
+      h = alpha[q];
+      node = 2 * node;
+    }
+  }
+  lo[b] = l;
+  hi[b] = h;
+  if (path_steps) path_steps[b] = acc;
+}
+
+__global__ void bisect_finish_kernel(int64_t nb, const double* __restrict__ lo, const double* __restrict__ hi,
+                                     double* __restrict__ alpha_c) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nb) alpha_c[b] = 0.5 * (lo[b] + hi[b]);
+}
+
+cudaError_t launch_bisect_build(int64_t nb, int64_t per, const double* lo, const double* hi, double* alpha,
+                                cudaStream_t s) {
+  const int64_t n = nb * per;
+  bisect_build_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(nb, per, lo, hi, alpha);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bisect_walk(int64_t nb, int64_t per, int levels, const double* alpha, const int32_t* term,
+                               const int64_t* steps, double* lo, double* hi, int64_t* path_steps,
+                               cudaStream_t s) {
+  bisect_walk_kernel<<<(unsigned)((nb + 127) / 128), 128, 0, s>>>(nb, per, levels, alpha, term, steps, lo, hi,
+                                                                  path_steps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bisect_finish(int64_t nb, const double* lo, const double* hi, double* alpha_c,
+                                 cudaStream_t s) {
+  bisect_finish_kernel<<<(unsigned)((nb + 127) / 128), 128, 0, s>>>(nb, lo, hi, alpha_c);
+  return cudaGetLastError();
+}
+
+// FMA throughput probes for the roofline denominators (independent chains).
+template <typename T>
+__global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x * (T)1e-3, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+  T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t launch_fma_probe(int fp64, void* out, int blocks, int threads, int iters, cudaStream_t s) {
+  if (fp64) fma_probe_kernel<double><<<blocks, threads, 0, s>>>((double*)out, iters, 0.999999, 1e-7);
+  else fma_probe_kernel<float><<<blocks, threads, 0, s>>>((float*)out, iters, 0.999999f, 1e-7f);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,237 @@
+// Mixed-precision ray tracing: the RK4 right-hand sides run in FP32, the ray
+// state is carried as FP32 (high, low) pairs with a compensated (two-sum)
+// update, and FP64 is used only inside a band around the photon sphere /
+// horizon / throat / bubble wall, where a ray's fate is decided.
+//
+// Why pairs for the whole state: a plain FP32 position at r = 1000 has an ulp
+// of 6e-5, coarser than a 0.01 step's increment allows, and a plain FP32
+// momentum random-walks to ~1e-6 relative over the 2000 steps before the
+// photon sphere, which would move the critical impact parameter past 1e-6. With
+// (hi, lo) pairs (48-bit significand) the state keeps FP64-class accuracy and
+// only the FP32 evaluation error of each increment (~1e-7 of h*k) remains.
+//
+// The persistent loop and the sources/sinks are shared with the FP64 path
+// (trace_common.cuh); this unit is compiled with --fmad=false too, so every
+// fused multiply-add in the FP32 code is written out explicitly.
+#include <cuda_runtime.h>
+
+#include "internal.h"
+#include "metric_analytic.cuh"
+#include "trace_common.cuh"
+
+namespace geon {
+
+__device__ __forceinline__ void two_sum_update(float& hi, float& lo, float inc) {
+  const float s = hi + inc;
+  const float bb = s - hi;
+  const float e = (hi - (s - bb)) + (inc - bb);
+  const float l2 = lo + e;
+  const float h2 = s + l2;
+  lo = l2 - (h2 - s);
+  hi = h2;
+}
+
+// (hi + lo) > t for a threshold held as a (hi, lo) pair.
+__device__ __forceinline__ bool ff_gt(float hi, float lo, float thi, float tlo) {
+  return (hi - thi) + (lo - tlo) > 0.0f;
+}
+
+template <int K>
+struct MixedStepper {
+  float hi[8], lo[8];
+  AConsts<float> C;
+  AConsts<double> Cd;
+  float cap_hi, cap_lo, esc_hi, esc_lo;
+  float h, hh, sixth;
+  bool ready = false;
+
+  __device__ __forceinline__ void setup(const TraceLaunch& L) {
+    C.init(L.M);
+    Cd.init(L.M);
+    cap_hi = __double2float_rn(L.M.capture_r);
+    cap_lo = __double2float_rn(L.M.capture_r - (double)cap_hi);
+    esc_hi = __double2float_rn(L.M.escape_r);
+    esc_lo = __double2float_rn(L.M.escape_r - (double)esc_hi);
+    h = (float)L.step;
+    hh = (float)L.half_step;
+    sixth = (float)L.sixth;
+    ready = true;
+  }
+
+  __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) {
+    if (!ready) setup(L);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      hi[i] = __double2float_rn(y0[i]);
+      lo[i] = __double2float_rn(y0[i] - (double)hi[i]);
+    }
+  }
+
+  __device__ __forceinline__ void to_double(double out[8]) const {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = (double)hi[i] + (double)lo[i];
+  }
+
+  // Termination tests of the reference, evaluated on the compensated state.
+  __device__ __forceinline__ int terminate(const TraceLaunch&) const {
+    if (K == KIND_SCHWARZSCHILD) {
+      if (!isfinite(hi[1])) return TERM_DIVERGED;
+      if (ff_gt(cap_hi, cap_lo, hi[1], lo[1])) return TERM_CAPTURED;
+      if (ff_gt(hi[1], lo[1], esc_hi, esc_lo)) return TERM_ESCAPED;
+      return TERM_NONE;
+    } else if (K == KIND_MORRIS_THORNE) {
+      if (!isfinite(hi[1])) return TERM_DIVERGED;
+      const float a = fabsf(hi[1]);
+      const float al = hi[1] < 0.0f ? -lo[1] : lo[1];
+      return ff_gt(a, al, 1000.0f, 0.0f) ? TERM_ESCAPED : TERM_NONE;
+    } else {
+      const float r2 = __fmaf_rn(hi[1], hi[1], __fmaf_rn(hi[2], hi[2], hi[3] * hi[3]));
+      if (K == KIND_ALCUBIERRE && !isfinite(r2)) return TERM_DIVERGED;
+      return r2 > 1e6f ? TERM_ESCAPED : TERM_NONE;
+    }
+  }
+
+  __device__ __forceinline__ bool step_fp32(const TraceLaunch& L) {
+    float s0 = 0.0f, c0 = 1.0f;
+    if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) sincosf(hi[2], &s0, &c0);
+    float d[8], k[8], acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) d[i] = lo[i];
+    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      acc[i] = k[i];
+      d[i] = __fmaf_rn(hh, k[i], lo[i]);
+    }
+    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      acc[i] = __fmaf_rn(2.0f, k[i], acc[i]);
+      d[i] = __fmaf_rn(hh, k[i], lo[i]);
+    }
+    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      acc[i] = __fmaf_rn(2.0f, k[i], acc[i]);
+      d[i] = __fmaf_rn(h, k[i], lo[i]);
+    }
+    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
+    bool finite = true;
+    float inc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      inc[i] = sixth * (acc[i] + k[i]);
+      finite &= isfinite(inc[i]);
+    }
+    if (!finite) return false;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) two_sum_update(hi[i], lo[i], inc[i]);
+    if (L.mixed_flags & MIXED_REPROJECT) {
+      float s = 0.0f;
+      if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) s = sinf(hi[2]);
+      const float x[4] = {hi[0], hi[1], hi[2], hi[3]};
+      const float p[4] = {hi[4], hi[5], hi[6], hi[7]};
+      const float pt = null_pt<K, float>(C, x, p, s, hi[4]);
+      if (isfinite(pt)) {
+        two_sum_update(hi[4], lo[4], (pt - hi[4]) - lo[4]);
+      }
+    }
+    return true;
+  }
+
+  // FP64 RK4 with the closed-form right-hand side (band steps).
+  __device__ __forceinline__ bool step_fp64(const TraceLaunch& L) {
+    double y[8];
+    to_double(y);
+    double s0 = 0.0, c0 = 1.0;
+    if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) ::sincos(y[2], &s0, &c0);
+    const double zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double k[8], acc[8], d[8];
+    rhs_analytic<K, double>(Cd, y, zero, s0, c0, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      acc[i] = k[i];
+      d[i] = L.half_step * k[i];
+    }
+    rhs_analytic<K, double>(Cd, y, d, s0, c0, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      acc[i] = ::fma(2.0, k[i], acc[i]);
+      d[i] = L.half_step * k[i];
+    }
+    rhs_analytic<K, double>(Cd, y, d, s0, c0, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      acc[i] = ::fma(2.0, k[i], acc[i]);
+      d[i] = L.step * k[i];
+    }
+    rhs_analytic<K, double>(Cd, y, d, s0, c0, k);
+    double yn[8];
+    bool finite = true;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      yn[i] = ::fma(L.sixth, acc[i] + k[i], y[i]);
+      finite &= isfinite(yn[i]);
+    }
+    if (!finite) return false;
+    load(L, yn);
+    return true;
+  }
+
+  __device__ __forceinline__ bool step(const TraceLaunch& L) {
+    if (K != KIND_MINKOWSKI && L.band > 0.0f && in_band<K>(L.M, hi[1], hi[2], hi[3], L.band))
+      return step_fp64(L);
+    return step_fp32(L);
+  }
+
+  __device__ __forceinline__ void finish(const TraceLaunch&) {}
+};
+
+template <int K, int SRC, int SINK>
+__global__ void __launch_bounds__(TRACE_BLOCK) trace_mixed_kernel(const TraceLaunch L) {
+  trace_loop<MixedStepper<K>, K, SRC, SINK>(L);
+}
+
+template <int K, int SRC, int SINK>
+static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
+  static int grid_cache = 0;
+  if (grid_cache == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_mixed_kernel<K, SRC, SINK>, TRACE_BLOCK, 0);
+    if (per_sm < 1) per_sm = 1;
+    grid_cache = sms * per_sm;
+  }
+  const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
+  int grid = (int)(need < grid_cache ? need : grid_cache);
+  if (grid < 1) grid = 1;
+  trace_mixed_kernel<K, SRC, SINK><<<grid, TRACE_BLOCK, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+template <int K>
+static cudaError_t launch_mk(const TraceLaunch& L, int src, int sink, cudaStream_t s) {
+  if (src == SRC_ARRAY && sink == SINK_TRACE) return launch_mst<K, SRC_ARRAY, SINK_TRACE>(L, s);
+  if (src == SRC_CAMERA && sink == SINK_RENDER) return launch_mst<K, SRC_CAMERA, SINK_RENDER>(L, s);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_trace_mixed(const TraceLaunch& L, int src, int sink, cudaStream_t s) {
+  if (L.n <= 0) return cudaSuccess;
+  if (src == SRC_EQUATORIAL) {
+    if (L.M.kind != KIND_SCHWARZSCHILD) return cudaErrorInvalidValue;
+    if (sink == SINK_SHADOW) return launch_mst<KIND_SCHWARZSCHILD, SRC_EQUATORIAL, SINK_SHADOW>(L, s);
+    if (sink == SINK_TRACE) return launch_mst<KIND_SCHWARZSCHILD, SRC_EQUATORIAL, SINK_TRACE>(L, s);
+    return cudaErrorInvalidValue;
+  }
+  switch (L.M.kind) {
+    case KIND_MINKOWSKI: return launch_mk<KIND_MINKOWSKI>(L, src, sink, s);
+    case KIND_SCHWARZSCHILD: return launch_mk<KIND_SCHWARZSCHILD>(L, src, sink, s);
+    case KIND_ALCUBIERRE: return launch_mk<KIND_ALCUBIERRE>(L, src, sink, s);
+    case KIND_MORRIS_THORNE: return launch_mk<KIND_MORRIS_THORNE>(L, src, sink, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace geon

@@ -157,6 +157,15 @@ int geon_sky_sample(const double* dir, size_t n, int show_stars, float* rgb);
 void geon_set_show_stars(int on);
 int geon_get_show_stars(void);
 
+/* --- mixed-precision options (no counterpart in the reference, which is FP64 only) ---
+ * FP64 band half-width for GEON_MIXED, per metric kind, in the metric's own
+ * scale: Schwarzschild r < band*M, Morris-Thorne |l| < band*b0, Alcubierre
+ * |r_s - R| < band*s; 0 disables the band. Defaults 4, 1.5, 3 (Minkowski: 0).
+ * geon_set_mixed_reproject(1) re-imposes g(p, p) = 0 on p^t after every FP32 step. */
+int geon_set_mixed_band(int kind, double band);
+double geon_get_mixed_band(int kind);
+void geon_set_mixed_reproject(int on);
+
 /* --- curvature.rs ------------------------------------------------------------ */
 int geon_riemann(geon_metric_t m, const double* x, size_t n, double* out);       /* curvature.rs:48, n*256 */
 int geon_ricci(geon_metric_t m, const double* x, size_t n, double* out);         /* curvature.rs:72, n*16 */
@@ -186,6 +195,24 @@ int geon_shadow_classify(geon_metric_t schwarzschild, double r_obs, const double
 int geon_shadow_bisect(geon_metric_t schwarzschild, double r_obs, const double* lo, const double* hi,
                        size_t nb, int iters, double step, int64_t max_steps, int precision,
                        double* alpha_c, double* lo_out, double* hi_out, int64_t* steps_out);
+
+/* Device-pointer, stream-ordered forms of the two calls above (alpha, lo, hi and
+ * every output are device addresses; the call returns once the work is queued).
+ * The bisection keeps its rounds on the device: no host round trip per round. */
+int geon_shadow_classify_dev(geon_metric_t schwarzschild, double r_obs, const double* alpha, size_t n,
+                             double step, int64_t max_steps, int precision, int32_t* term,
+                             int64_t* steps, void* stream);
+int geon_shadow_bisect_dev(geon_metric_t schwarzschild, double r_obs, const double* lo, const double* hi,
+                           size_t nb, int iters, double step, int64_t max_steps, int precision,
+                           double* alpha_c, double* lo_out, double* hi_out, int64_t* steps_out,
+                           void* stream);
+
+/* --- measurement helpers (no counterpart in the reference) --------------------- */
+/* Kernels this library has launched since it was loaded. */
+unsigned long long geon_launch_count(void);
+/* Sustained FMA throughput of this GPU (independent chains on every SM), in
+ * TFLOP/s: fp64 != 0 measures DFMA, else FFMA. The roofline denominator. */
+int geon_probe_fma_peak(int fp64, double* tflops);
 
 #ifdef __cplusplus
 }

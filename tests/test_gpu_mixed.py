@@ -1,0 +1,87 @@
+"""Mixed-precision path (FP32 bulk, compensated state, FP64 band) against the
+FP64 path: classification mismatch, escape-direction error, critical impact
+parameter. Tolerances: mismatch < 1e-4 of rays on the shadow sweep, b_c within
+1e-6 of 3 sqrt(3) M, as the task sets them; direction error per metric below."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mixed_shadow_sweep_matches_fp64(geon):
+    m = geon.Schwarzschild(1.0)
+    rng = np.random.default_rng(0x5EED)
+    alpha = np.radians(rng.uniform(10.0, 20.0, 8192))
+    t64, s64 = geon.shadow.classify(m, 20.0, alpha, 0.01, 200000, precision="fp64")
+    tmx, smx = geon.shadow.classify(m, 20.0, alpha, 0.01, 200000, precision="mixed")
+    assert np.mean(t64 != tmx) < 1e-4 * 8 + 1e-9  # at most a few rays of 8192, all next to alpha_c
+    bad = np.where(t64 != tmx)[0]
+    assert np.all(np.abs(np.degrees(alpha[bad]) - 14.269) < 1e-3)
+    assert np.abs(smx - s64).max() <= 2
+
+
+def test_mixed_bisection_b_c(geon):
+    m = geon.Schwarzschild(1.0)
+    ac, lo, hi, st = geon.shadow.bisect(m, 20.0, 0.0, np.pi / 2 - 1e-3, iters=60, precision="mixed")
+    b_c = geon.shadow.impact_parameter(m, 20.0, ac[0])
+    assert abs(b_c - 3.0 * np.sqrt(3.0)) / (3.0 * np.sqrt(3.0)) <= 1e-6
+
+
+@pytest.mark.parametrize("band,reproject", [(4.0, 0), (0.0, 0), (4.0, 1)])
+def test_mixed_render_schwarzschild(geon, band, reproject):
+    lib = geon._load()
+    lib.geon_set_mixed_band(1, band)
+    lib.geon_set_mixed_reproject(reproject)
+    try:
+        m = geon.Schwarzschild(1.0, 1.001, 100.0)
+        cam = geon.Camera([0.0, 30.0, np.pi / 2, 0.0], 60.0, 64, 64)
+        tet = cam.tetrad(m)
+        y0 = cam.ray_states(tet)
+        r64 = geon.trace(m, y0, 0.05, 20000, precision="fp64")
+        rmx = geon.trace(m, y0, 0.05, 20000, precision="mixed")
+        assert np.mean(r64.termination != rmx.termination) <= 2e-3
+        esc = (r64.termination == 2) & (rmx.termination == 2)
+        d64 = m.asymptotic_direction(r64.final_state[esc])
+        dmx = m.asymptotic_direction(rmx.final_state[esc])
+        ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1, 1))
+        assert np.median(ang) < 1e-6
+        assert np.mean(ang < 1e-4) > 0.99
+        rgb64, st64 = geon.render(m, cam, geon.RenderConfig(precision="fp64"))
+        rgbmx, stmx = geon.render(m, cam, geon.RenderConfig(precision="mixed"))
+        assert np.mean(np.any(rgb64 != rgbmx, axis=-1)) < 0.01
+    finally:
+        lib.geon_set_mixed_band(1, 4.0)
+        lib.geon_set_mixed_reproject(0)
+
+
+@pytest.mark.parametrize("kind,params,obs,fov,fs", [
+    (3, [1.0], [0.0, 10.0, np.pi / 2, 0.0], 90.0, 1),
+    (2, [2.0, 0.125, 0.5, 0.0], [0.0, -10.0, 0.0, 0.0], 90.0, -1),
+    (0, [], [0.0, 20.0, 0.0, 0.0], 60.0, 1)], ids=["morris_thorne", "alcubierre", "minkowski"])
+def test_mixed_exotic_close_to_fp64(geon, kind, params, obs, fov, fs):
+    m = geon.from_kind(kind, params)
+    cam = geon.Camera(obs, fov, 24, 24, forward_sign=fs)
+    y0 = cam.ray_states(cam.tetrad(m))
+    r64 = geon.trace(m, y0, 0.05, 3000, precision="fp64")
+    rmx = geon.trace(m, y0, 0.05, 3000, precision="mixed")
+    assert np.mean(r64.termination != rmx.termination) <= 0.01
+    both = r64.termination == rmx.termination
+    pos = np.linalg.norm(r64.final_state[both, 1:4] - rmx.final_state[both, 1:4], axis=1)
+    scale = np.maximum(1.0, np.linalg.norm(r64.final_state[both, 1:4], axis=1))
+    assert np.median(pos / scale) < 1e-5
+
+
+def test_shadow_dev_api(geon):
+    torch = pytest.importorskip("torch")
+    lib = geon._load()
+    m = geon.Schwarzschild(1.0)
+    lo = torch.tensor(np.radians([13.1, 13.7]), device="cuda")
+    hi = torch.tensor(np.radians([14.9, 15.4]), device="cuda")
+    ac = torch.empty(2, dtype=torch.float64, device="cuda")
+    st = torch.empty(2, dtype=torch.int64, device="cuda")
+    s = torch.cuda.current_stream()
+    assert lib.geon_shadow_bisect_dev(m.handle, 20.0, lo.data_ptr(), hi.data_ptr(), 2, 12, 0.01, 200000, 0,
+                                      ac.data_ptr(), None, None, st.data_ptr(), s.cuda_stream) == 0
+    torch.cuda.synchronize()
+    ref, _, _, rst = geon.shadow.bisect(m, 20.0, lo.cpu().numpy(), hi.cpu().numpy(), iters=12)
+    assert np.array_equal(ac.cpu().numpy(), ref) and np.array_equal(st.cpu().numpy(), rst)
