@@ -81,6 +81,7 @@ SIGNATURES = {
     "geon_set_mixed_band": (ctypes.c_int, [ctypes.c_int, ctypes.c_double]),
     "geon_get_mixed_band": (ctypes.c_double, [ctypes.c_int]),
     "geon_set_mixed_reproject": (None, [ctypes.c_int]),
+    "geon_set_persistent_reserve": (None, [ctypes.c_int]),
     "geon_riemann": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
     "geon_ricci": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
     "geon_ricci_scalar": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),

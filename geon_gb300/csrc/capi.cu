@@ -26,8 +26,9 @@ thread_local std::string g_last_error;
 std::atomic<int> g_show_stars{1};
 // Mixed-precision options: FP64 band half-width per metric kind (in units of
 // M, b0, s; 0 disables) and the null re-projection switch.
-std::atomic<float> g_band[4] = {{0.0f}, {4.0f}, {3.0f}, {1.5f}};
+std::atomic<float> g_band[4] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
 std::atomic<int> g_reproject{0};
+std::atomic<int> g_reserve{0};
 // Kernels launched by this library since load (ours only; memsets excluded).
 std::atomic<unsigned long long> g_launches{0};
 inline void counted(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -134,6 +135,7 @@ TraceLaunch base_launch(geon_metric_t m, double step, int64_t max_steps) {
   L.max_steps = max_steps;
   L.band = g_band[m->desc.kind].load();
   L.mixed_flags = g_reproject.load() ? MIXED_REPROJECT : 0;
+  L.reserve_per_sm = g_reserve.load();
   return L;
 }
 
@@ -192,6 +194,8 @@ double geon_get_mixed_band(int kind) {
 }
 
 void geon_set_mixed_reproject(int on) { g_reproject.store(on ? 1 : 0); }
+
+void geon_set_persistent_reserve(int blocks_per_sm) { g_reserve.store(blocks_per_sm < 0 ? 0 : blocks_per_sm); }
 int geon_get_show_stars(void) { return g_show_stars.load(); }
 
 int geon_metric_create(int kind, const double* params, int nparams, geon_metric_t* out) {

@@ -68,6 +68,7 @@ struct TraceLaunch {
   float diverged_rgb[3];  // RenderConfig::diverged_rgb (render.rs:25)
   // mixed precision
   float band;          // FP64 band half-width in the metric's own scale (0 = no band)
+  int reserve_per_sm;  // persistent grid leaves this many blocks per SM free
   int mixed_flags;     // MIXED_* bits
   // work queue
   unsigned long long* queue;  // next unclaimed ray index

@@ -110,10 +110,12 @@ __device__ __forceinline__ void store_ray(const TraceLaunch& L, int64_t ray, int
 }
 
 constexpr int TRACE_BLOCK = 128;
+enum : int { STEP_NONFINITE = 0, STEP_OK = 1, STEP_HORIZON = 2 };
 
 // geodesic.rs:62-117 for every ray of the job, persistent over a work queue.
 // Stepper owns the ray state: load(y0), to_double(y), terminate(L), step(L)
-// (true = advanced, false = the new state was not finite; state unchanged).
+// returning STEP_OK (advanced), STEP_NONFINITE (state unchanged: Diverged) or
+// STEP_HORIZON (state unchanged: Captured after this step).
 template <class Stepper, int K, int SRC, int SINK>
 __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
   const unsigned FULL = 0xffffffffu;
@@ -152,8 +154,15 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
       } else {
         t = st.terminate(L);
         if (t == TERM_NONE) {
-          if (st.step(L)) ++n;
-          else t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
+          const int r = st.step(L);
+          if (r == STEP_OK) {
+            ++n;
+          } else if (r == STEP_NONFINITE) {
+            t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
+          } else {
+            t = TERM_CAPTURED;
+            taken = n + 1;
+          }
         }
       }
       if (t != TERM_NONE) {

@@ -27,16 +27,16 @@ struct Fp64Stepper {
     for (int i = 0; i < 8; ++i) out[i] = y[i];
   }
   __device__ __forceinline__ int terminate(const TraceLaunch& L) const { return metric_terminate<K>(L.M, y); }
-  __device__ __forceinline__ bool step(const TraceLaunch& L) {
+  __device__ __forceinline__ int step(const TraceLaunch& L) {
     double yn[8];
     singular |= !rk4_step<K>(L.M, y, L.step, L.half_step, L.sixth, yn);
     bool finite = true;
 #pragma unroll
     for (int i = 0; i < 8; ++i) finite &= isfinite(yn[i]);
-    if (!finite) return false;
+    if (!finite) return STEP_NONFINITE;
 #pragma unroll
     for (int i = 0; i < 8; ++i) y[i] = yn[i];
-    return true;
+    return STEP_OK;
   }
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
@@ -50,18 +50,20 @@ __global__ void __launch_bounds__(TRACE_BLOCK) trace_fp64_kernel(const TraceLaun
 
 template <int K, int SRC, int SINK>
 static cudaError_t launch_kst(const TraceLaunch& L, cudaStream_t s) {
-  static int grid_cache = 0;
-  if (grid_cache == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
+  static int sms = 0, per_sm = 0;
+  if (sms == 0) {
+    int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_fp64_kernel<K, SRC, SINK>,
-                                                  TRACE_BLOCK, 0);
-    if (per_sm < 1) per_sm = 1;
-    grid_cache = sms * per_sm;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_fp64_kernel<K, SRC, SINK>, TRACE_BLOCK, 0);
+    per_sm = occ < 1 ? 1 : occ;
   }
-  int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
-  int grid = (int)(need < grid_cache ? need : grid_cache);
+  // persistent grid: every resident slot, minus the blocks per SM the caller
+  // keeps free for a concurrent job
+  const int use = per_sm - L.reserve_per_sm < 1 ? 1 : per_sm - L.reserve_per_sm;
+  const int64_t slots = (int64_t)sms * use;
+  const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
+  int grid = (int)(need < slots ? need : slots);
   if (grid < 1) grid = 1;
   trace_fp64_kernel<K, SRC, SINK><<<grid, TRACE_BLOCK, 0, s>>>(L);
   return cudaGetLastError();

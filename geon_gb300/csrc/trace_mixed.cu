@@ -91,7 +91,12 @@ struct MixedStepper {
     }
   }
 
-  __device__ __forceinline__ bool step_fp32(const TraceLaunch& L) {
+  // Returns STEP_OK, STEP_NONFINITE (state unchanged) or STEP_HORIZON: an RK4
+  // stage of a Schwarzschild ray reached r <= 2M, where f = 1 - 2M/r changes
+  // sign and the fixed step has no meaning; the ray has crossed the horizon and
+  // is reported Captured. (The FP64 path keeps the reference's behaviour: such a
+  // step overflows or throws the ray to r ~ 1e30, reported Diverged or Escaped.)
+  __device__ __forceinline__ int step_fp32(const TraceLaunch& L) {
     float s0 = 0.0f, c0 = 1.0f;
     if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) sincosf(hi[2], &s0, &c0);
     float d[8], k[8], acc[8];
@@ -103,19 +108,23 @@ struct MixedStepper {
       acc[i] = k[i];
       d[i] = __fmaf_rn(hh, k[i], lo[i]);
     }
+    float rmin = d[1];  // lowest stage radius, as an offset from hi[1]
     rhs_analytic<K, float>(C, hi, d, s0, c0, k);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       acc[i] = __fmaf_rn(2.0f, k[i], acc[i]);
       d[i] = __fmaf_rn(hh, k[i], lo[i]);
     }
+    rmin = fminf(rmin, d[1]);
     rhs_analytic<K, float>(C, hi, d, s0, c0, k);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       acc[i] = __fmaf_rn(2.0f, k[i], acc[i]);
       d[i] = __fmaf_rn(h, k[i], lo[i]);
     }
+    rmin = fminf(rmin, d[1]);
     rhs_analytic<K, float>(C, hi, d, s0, c0, k);
+    if (K == KIND_SCHWARZSCHILD && !(hi[1] + rmin > C.two_m)) return STEP_HORIZON;
     bool finite = true;
     float inc[8];
 #pragma unroll
@@ -123,7 +132,7 @@ struct MixedStepper {
       inc[i] = sixth * (acc[i] + k[i]);
       finite &= isfinite(inc[i]);
     }
-    if (!finite) return false;
+    if (!finite) return STEP_NONFINITE;
 #pragma unroll
     for (int i = 0; i < 8; ++i) two_sum_update(hi[i], lo[i], inc[i]);
     if (L.mixed_flags & MIXED_REPROJECT) {
@@ -136,11 +145,11 @@ struct MixedStepper {
         two_sum_update(hi[4], lo[4], (pt - hi[4]) - lo[4]);
       }
     }
-    return true;
+    return STEP_OK;
   }
 
   // FP64 RK4 with the closed-form right-hand side (band steps).
-  __device__ __forceinline__ bool step_fp64(const TraceLaunch& L) {
+  __device__ __forceinline__ int step_fp64(const TraceLaunch& L) {
     double y[8];
     to_double(y);
     double s0 = 0.0, c0 = 1.0;
@@ -153,19 +162,23 @@ struct MixedStepper {
       acc[i] = k[i];
       d[i] = L.half_step * k[i];
     }
+    double rmin = d[1];
     rhs_analytic<K, double>(Cd, y, d, s0, c0, k);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       acc[i] = ::fma(2.0, k[i], acc[i]);
       d[i] = L.half_step * k[i];
     }
+    rmin = fmin(rmin, d[1]);
     rhs_analytic<K, double>(Cd, y, d, s0, c0, k);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       acc[i] = ::fma(2.0, k[i], acc[i]);
       d[i] = L.step * k[i];
     }
+    rmin = fmin(rmin, d[1]);
     rhs_analytic<K, double>(Cd, y, d, s0, c0, k);
+    if (K == KIND_SCHWARZSCHILD && !(y[1] + rmin > Cd.two_m)) return STEP_HORIZON;
     double yn[8];
     bool finite = true;
 #pragma unroll
@@ -173,12 +186,12 @@ struct MixedStepper {
       yn[i] = ::fma(L.sixth, acc[i] + k[i], y[i]);
       finite &= isfinite(yn[i]);
     }
-    if (!finite) return false;
+    if (!finite) return STEP_NONFINITE;
     load(L, yn);
-    return true;
+    return STEP_OK;
   }
 
-  __device__ __forceinline__ bool step(const TraceLaunch& L) {
+  __device__ __forceinline__ int step(const TraceLaunch& L) {
     if (K != KIND_MINKOWSKI && L.band > 0.0f && in_band<K>(L.M, hi[1], hi[2], hi[3], L.band))
       return step_fp64(L);
     return step_fp32(L);
@@ -194,17 +207,20 @@ __global__ void __launch_bounds__(TRACE_BLOCK) trace_mixed_kernel(const TraceLau
 
 template <int K, int SRC, int SINK>
 static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
-  static int grid_cache = 0;
-  if (grid_cache == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
+  static int sms = 0, per_sm = 0;
+  if (sms == 0) {
+    int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_mixed_kernel<K, SRC, SINK>, TRACE_BLOCK, 0);
-    if (per_sm < 1) per_sm = 1;
-    grid_cache = sms * per_sm;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_mixed_kernel<K, SRC, SINK>, TRACE_BLOCK, 0);
+    per_sm = occ < 1 ? 1 : occ;
   }
+  // persistent grid: every resident slot, minus the blocks per SM the caller
+  // keeps free for a concurrent job
+  const int use = per_sm - L.reserve_per_sm < 1 ? 1 : per_sm - L.reserve_per_sm;
+  const int64_t slots = (int64_t)sms * use;
   const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
-  int grid = (int)(need < grid_cache ? need : grid_cache);
+  int grid = (int)(need < slots ? need : slots);
   if (grid < 1) grid = 1;
   trace_mixed_kernel<K, SRC, SINK><<<grid, TRACE_BLOCK, 0, s>>>(L);
   return cudaGetLastError();

@@ -160,11 +160,17 @@ int geon_get_show_stars(void);
 /* --- mixed-precision options (no counterpart in the reference, which is FP64 only) ---
  * FP64 band half-width for GEON_MIXED, per metric kind, in the metric's own
  * scale: Schwarzschild r < band*M, Morris-Thorne |l| < band*b0, Alcubierre
- * |r_s - R| < band*s; 0 disables the band. Defaults 4, 1.5, 3 (Minkowski: 0).
+ * |r_s - R| < band*s; 0 (the default) disables the band: with the compensated
+ * FP32 state the band is not needed for accuracy and costs warp divergence.
  * geon_set_mixed_reproject(1) re-imposes g(p, p) = 0 on p^t after every FP32 step. */
 int geon_set_mixed_band(int kind, double band);
 double geon_get_mixed_band(int kind);
 void geon_set_mixed_reproject(int on);
+/* Trace kernels are persistent (one grid fills every SM and pulls rays from a
+ * device work queue). To let another job run beside one (e.g. bisections next
+ * to a sweep), calls made after this keep `blocks_per_sm` resident slots per SM
+ * free. Default 0. */
+void geon_set_persistent_reserve(int blocks_per_sm);
 
 /* --- curvature.rs ------------------------------------------------------------ */
 int geon_riemann(geon_metric_t m, const double* x, size_t n, double* out);       /* curvature.rs:48, n*256 */
