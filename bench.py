@@ -155,6 +155,10 @@ def main():
     ap.add_argument("--cpu-rays", type=int, default=4096)
     ap.add_argument("--fp64-sample", type=int, default=32, help="FP64 leg traces every k-th sweep ray")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 leg, accuracy, e2e and CPU legs")
+    # small cases for profiling only (they change the workload; never a bench line)
+    ap.add_argument("--rays", type=int, default=N_SWEEP, help="profiling: sweep size")
+    ap.add_argument("--sweep-only", action="store_true", help="profiling: no bisections")
+    ap.add_argument("--escape-radius", type=float, default=SCHW[2], help="profiling: escape radius in M")
     args = ap.parse_args()
     assert args.warmup >= 3, "at least 3 warm-up steps"
 
@@ -175,15 +179,17 @@ def main():
     from geon_gb300 import _ffi
     lib = _ffi.load()
     prec = 1 if args.precision == "mixed" else 0
-    m = geon.Schwarzschild(*SCHW)
+    m = geon.Schwarzschild(SCHW[0], SCHW[1], args.escape_radius)
     h = m.handle
     alpha, lo, hi = workload(0x5EED + rank)
+    n_sweep = args.rays
+    alpha = alpha[:n_sweep]
     dev = torch.device("cuda", local)
     d_alpha = torch.tensor(alpha, device=dev)
     d_lo = torch.tensor(lo, device=dev)
     d_hi = torch.tensor(hi, device=dev)
-    d_term = torch.empty(N_SWEEP, dtype=torch.int32, device=dev)
-    d_steps = torch.empty(N_SWEEP, dtype=torch.int64, device=dev)
+    d_term = torch.empty(n_sweep, dtype=torch.int32, device=dev)
+    d_steps = torch.empty(n_sweep, dtype=torch.int64, device=dev)
     d_ac = torch.empty(N_BRACKETS, dtype=torch.float64, device=dev)
     d_bst = torch.empty(N_BRACKETS, dtype=torch.int64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
@@ -204,14 +210,15 @@ def main():
         sb.wait_stream(main)
         ea0.record(sa)
         lib.geon_set_persistent_reserve(RESERVE)  # leave room on every SM for the bisection rounds
-        check(lib.geon_shadow_classify_dev(h, R_OBS, d_alpha.data_ptr(), N_SWEEP, STEP, MAX_STEPS, precision,
+        check(lib.geon_shadow_classify_dev(h, R_OBS, d_alpha.data_ptr(), n_sweep, STEP, MAX_STEPS, precision,
                                            d_term.data_ptr(), d_steps.data_ptr(), sa.cuda_stream))
         lib.geon_set_persistent_reserve(0)
         ea1.record(sa)
         eb0.record(sb)
-        check(lib.geon_shadow_bisect_dev(h, R_OBS, d_lo.data_ptr(), d_hi.data_ptr(), N_BRACKETS, ITERS, STEP,
-                                         MAX_STEPS, precision, d_ac.data_ptr(), None, None, d_bst.data_ptr(),
-                                         sb.cuda_stream))
+        if not args.sweep_only:
+            check(lib.geon_shadow_bisect_dev(h, R_OBS, d_lo.data_ptr(), d_hi.data_ptr(), N_BRACKETS, ITERS, STEP,
+                                             MAX_STEPS, precision, d_ac.data_ptr(), None, None, d_bst.data_ptr(),
+                                             sb.cuda_stream))
         eb1.record(sb)
         main.wait_stream(sa)
         main.wait_stream(sb)
@@ -239,7 +246,7 @@ def main():
         times.append(ev[0].elapsed_time(ev[1]))
         sweep_ms.append(ev[2].elapsed_time(ev[3]))
         bis_ms.append(ev[4].elapsed_time(ev[5]))
-        total_steps += int(d_steps.sum().item()) + int(d_bst.sum().item())
+        total_steps += int(d_steps.sum().item()) + (0 if args.sweep_only else int(d_bst.sum().item()))
         flush.zero_()  # between timed iterations, outside the events
     barrier()
     launches = lib.geon_launch_count() - launches0
@@ -277,7 +284,7 @@ def main():
                 "peak_source": "measured in this run: FFMA/DFMA throughput probe (geon_probe_fma_peak); "
                                "MEASURED_PEAKS.json has no FP32/FP64 non-tensor peak"}
 
-    if not args.no_extras:
+    if not args.no_extras and n_sweep == N_SWEEP and not args.sweep_only and args.escape_radius == SCHW[2]:
         extras = extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_mixed, prec, dev, value)
 
     line = {
