@@ -102,6 +102,9 @@ SIGNATURES = {
     "geon_shadow_bisect_dev": (ctypes.c_int, [c_void_p, ctypes.c_double, c_void_p, c_void_p, c_size_t,
                                               ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
                                               c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "geon_shadow_bisect_dev_noalloc": (ctypes.c_int, [c_void_p, ctypes.c_double, c_void_p, c_void_p, c_size_t,
+                                                      ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
+                                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "geon_launch_count": (ctypes.c_ulonglong, []),
     "geon_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, c_double_p]),
 }

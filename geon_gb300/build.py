@@ -27,6 +27,7 @@ UNITS = [
     ("trace_mixed.cu", ["--fmad=false"]),
     ("curvature_fp64.cu", ["--fmad=false"]),
     ("capi.cu", ["--fmad=false"]),
+    ("noalloc.cu", ["--fmad=false"]),
 ]
 
 

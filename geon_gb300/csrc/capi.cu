@@ -146,12 +146,36 @@ cudaError_t launch_trace(const TraceLaunch& L, int precision, int src, int sink,
 
 bool valid_precision(int p) { return p == GEON_FP64 || p == GEON_MIXED; }
 
+// Levels of the speculative bisection tree traced per round: as many as keep
+// nb * (2^L - 1) launch angles within 16384 rays (at most 16).
+int64_t bisect_levels(size_t nb) {
+  const int64_t target_rays = 16384;
+  int L = 1;
+  while (L < 16 && (int64_t)nb * ((1LL << (L + 1)) - 1) <= target_rays) ++L;
+  return L;
+}
+
 int copy_out(void* host, const void* dev, size_t bytes, cudaStream_t s) {
   if (host && bytes) GEON_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s));
   return GEON_OK;
 }
 
 }  // namespace
+
+// Helpers for other translation units of the ABI (added entry points reuse the
+// handle, launch defaults, launch counter and error slot defined here).
+namespace geon {
+const MetricDesc* metric_desc(geon_metric_t m) { return m ? &m->desc : nullptr; }
+TraceLaunch trace_launch_defaults(geon_metric_t m, double step, int64_t max_steps) {
+  return base_launch(m, step, max_steps);
+}
+cudaError_t launch_trace_any(const TraceLaunch& L, int precision, int src, int sink, cudaStream_t s) {
+  return launch_trace(L, precision, src, sink, s);
+}
+void note_launches(unsigned long long n) { counted(n); }
+int set_last_error(int code, const char* msg) { return fail(code, msg); }
+int bisect_levels_for(size_t nb) { return (int)bisect_levels(nb); }
+}  // namespace geon
 
 // Kernels defined in trace_fp64.cu used only from here.
 namespace geon {
@@ -572,12 +596,6 @@ int geon_shadow_classify(geon_metric_t m, double r_obs, const double* alpha, siz
 // replays the sequential path through the tree. The result equals the
 // sequential loop bit for bit, with ceil(iters / L) dependent rounds instead of
 // iters, and no host round trip between rounds (3 launches per round).
-static int64_t bisect_levels(size_t nb) {
-  const int64_t target_rays = 16384;
-  int L = 1;
-  while (L < 16 && (int64_t)nb * ((1LL << (L + 1)) - 1) <= target_rays) ++L;
-  return L;
-}
 
 int geon_shadow_bisect_dev(geon_metric_t m, double r_obs, const double* lo, const double* hi, size_t nb,
                            int iters, double step, int64_t max_steps, int precision, double* alpha_c,
@@ -672,6 +690,7 @@ int geon_shadow_classify_dev(geon_metric_t m, double r_obs, const double* alpha,
 }
 
 unsigned long long geon_launch_count(void) { return g_launches.load(); }
+
 
 int geon_probe_fma_peak(int fp64, double* tflops) {
   if (!tflops) return fail(GEON_ERR_INVALID, "null output");

@@ -104,6 +104,14 @@ cudaError_t launch_curvature(const MetricDesc& M, int what, const double* x, int
                              const double* k, int64_t nk, int k_shared, double* out, int* flags,
                              cudaStream_t s);
 
+// ---- capi.cu helpers shared with other entry-point units ----
+const MetricDesc* metric_desc(geon_metric_t m);
+TraceLaunch trace_launch_defaults(geon_metric_t m, double step, int64_t max_steps);
+cudaError_t launch_trace_any(const TraceLaunch& L, int precision, int src, int sink, cudaStream_t s);
+void note_launches(unsigned long long n);
+int set_last_error(int code, const char* msg);
+int bisect_levels_for(size_t nb);
+
 // pointwise "what" codes
 enum : int { PW_G = 0, PW_DG = 1, PW_GINV = 2, PW_CHRISTOFFEL = 3, PW_TERMINATE = 4, PW_ASYM = 5 };
 

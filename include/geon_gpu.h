@@ -213,6 +213,22 @@ int geon_shadow_bisect_dev(geon_metric_t schwarzschild, double r_obs, const doub
                            double* alpha_c, double* lo_out, double* hi_out, int64_t* steps_out,
                            void* stream);
 
+/* geon_shadow_bisect_dev without any device allocation. No counterpart in the
+ * reference: it exists for callers that may not let a library allocate GPU
+ * memory while they run (a host that owns all device memory through its own
+ * pool, a real-time loop with no room for an allocator call, code that must not
+ * fail with "out of memory" mid-way). Its working memory is one fixed 512 KiB
+ * array compiled into the library, held on every GPU that loads the library
+ * until exit; at most 4096 brackets per call (larger: GEON_ERR_INVALID). The
+ * first call on each device looks up that array's device address; make it
+ * before any stream capture. Calls share the array: calls that overlap on the
+ * GPU race with each other, so order them on one stream. Same arguments and
+ * results as geon_shadow_bisect_dev. */
+int geon_shadow_bisect_dev_noalloc(geon_metric_t schwarzschild, double r_obs, const double* lo,
+                                   const double* hi, size_t nb, int iters, double step,
+                                   int64_t max_steps, int precision, double* alpha_c,
+                                   double* lo_out, double* hi_out, int64_t* steps_out, void* stream);
+
 /* --- measurement helpers (no counterpart in the reference) --------------------- */
 /* Kernels this library has launched since it was loaded. */
 unsigned long long geon_launch_count(void);
