@@ -185,6 +185,7 @@ def main():
     n_sweep = args.rays
     alpha = alpha[:n_sweep]
     dev = torch.device("cuda", local)
+    tuned = geon.autotune.autotune(geon.Schwarzschild(SCHW[0], SCHW[1], 100.0)) if prec == 1 else None
     d_alpha = torch.tensor(alpha, device=dev)
     d_lo = torch.tensor(lo, device=dev)
     d_hi = torch.tensor(hi, device=dev)
@@ -296,7 +297,8 @@ def main():
         "config": {"workload": "schwarzschild shadow sweep: 2^20 equatorial rays alpha~U[10,20] deg + 64 concurrent "
                                "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
                    "precision": args.precision, "rays_per_gpu": N_SWEEP, "bisections_per_gpu": N_BRACKETS,
-                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards"},
+                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards",
+                   "mixed_kernel_variant": None if tuned is None else tuned["variant"][1]},
         "latency": {"bisection_ms_p50": float(np.percentile(bis_ms, 50)),
                     "bisection_ms_p99": float(np.percentile(bis_ms, 99)),
                     "sweep_ms_p50": float(np.percentile(sweep_ms, 50)),

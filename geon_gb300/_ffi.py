@@ -43,6 +43,11 @@ class GeonRenderConfig(ctypes.Structure):
                 ("precision", ctypes.c_int32)]
 
 
+class GeonGrid(ctypes.Structure):
+    _fields_ = [("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3), ("n", ctypes.c_int64 * 3),
+                ("t", ctypes.c_double)]
+
+
 class GeonRenderStats(ctypes.Structure):
     _fields_ = [("captured", ctypes.c_int64), ("escaped", ctypes.c_int64),
                 ("diverged", ctypes.c_int64), ("max_null_residual", ctypes.c_double),
@@ -82,6 +87,10 @@ SIGNATURES = {
     "geon_get_mixed_band": (ctypes.c_double, [ctypes.c_int]),
     "geon_set_mixed_reproject": (None, [ctypes.c_int]),
     "geon_set_persistent_reserve": (None, [ctypes.c_int]),
+    "geon_set_mixed_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "geon_get_mixed_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "geon_autotune_mixed": (ctypes.c_int, [c_void_p, ctypes.c_int64, ctypes.c_int64, c_double_p,
+                                           ctypes.POINTER(ctypes.c_int)]),
     "geon_riemann": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
     "geon_ricci": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
     "geon_ricci_scalar": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),
@@ -91,6 +100,10 @@ SIGNATURES = {
                                             ctypes.c_int, c_double_p]),
     "geon_wec_contraction": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p, c_size_t,
                                             ctypes.c_int, c_double_p]),
+    "geon_curvature_grid": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonGrid), c_size_t, ctypes.c_uint64,
+                                           c_double_p, c_double_p, c_double_p]),
+    "geon_curvature_grid_dev": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonGrid), c_size_t, ctypes.c_uint64,
+                                               c_void_p, c_void_p, c_void_p, c_void_p]),
     "geon_equatorial_rays": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_size_t, c_double_p]),
     "geon_shadow_classify": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_size_t, ctypes.c_double,
                                             ctypes.c_int64, ctypes.c_int, c_int32_p, c_int64_p]),

@@ -37,6 +37,14 @@ struct CameraDesc {
 };
 
 enum : int { MIXED_REPROJECT = 1 };
+constexpr int MIXED_VARIANTS = 3;
+
+// A regular grid of points for curvature jobs (geon_grid of the ABI).
+struct GridDesc {
+  double lo[3], hi[3];
+  int64_t n[3];
+  double t;
+};
 
 // Sources of initial states.
 enum : int { SRC_ARRAY = 0, SRC_CAMERA = 1, SRC_EQUATORIAL = 2 };
@@ -69,6 +77,7 @@ struct TraceLaunch {
   // mixed precision
   float band;          // FP64 band half-width in the metric's own scale (0 = no band)
   int reserve_per_sm;  // persistent grid leaves this many blocks per SM free
+  int variant;         // mixed kernel register-cap variant (0: none, 1: 5 blocks/SM, 2: 6)
   int mixed_flags;     // MIXED_* bits
   // work queue
   unsigned long long* queue;  // next unclaimed ray index
@@ -103,6 +112,8 @@ cudaError_t launch_fma_probe(int fp64, void* out, int blocks, int threads, int i
 cudaError_t launch_curvature(const MetricDesc& M, int what, const double* x, int64_t n,
                              const double* k, int64_t nk, int k_shared, double* out, int* flags,
                              cudaStream_t s);
+cudaError_t launch_curvature_grid(const MetricDesc& M, const GridDesc& grid, int64_t nk, uint64_t seed,
+                                  double* einstein, double* nec, double* kout, int* flags, cudaStream_t s);
 
 // ---- capi.cu helpers shared with other entry-point units ----
 const MetricDesc* metric_desc(geon_metric_t m);

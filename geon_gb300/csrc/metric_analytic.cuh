@@ -34,8 +34,13 @@ struct AMath;
 template <>
 struct AMath<float> {
   static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-  static __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
-  static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+  // approximate reciprocal (one MUFU op, ~1 ulp): the RHS tolerates FP32 error
+  static __device__ __forceinline__ float rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float div(float a, float b) { return a * rcp(b); }
   static __device__ __forceinline__ float sqrt(float x) { return __fsqrt_rn(x); }
   static __device__ __forceinline__ float tanh(float x) { return tanhf(x); }
   static __device__ __forceinline__ void sincos(float x, float* s, float* c) { sincosf(x, s, c); }

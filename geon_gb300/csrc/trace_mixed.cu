@@ -21,14 +21,31 @@
 
 namespace geon {
 
+// (hi, lo) += inc, compensated. The rounding error of hi + inc is recovered
+// exactly (TwoSum, Knuth; or Fast2Sum, Dekker, when |hi| >= |inc| is known) and
+// accumulated into lo; hi is not renormalised here (see renormalise()).
 __device__ __forceinline__ void two_sum_update(float& hi, float& lo, float inc) {
   const float s = hi + inc;
   const float bb = s - hi;
   const float e = (hi - (s - bb)) + (inc - bb);
-  const float l2 = lo + e;
-  const float h2 = s + l2;
-  lo = l2 - (h2 - s);
-  hi = h2;
+  lo = lo + e;
+  hi = s;
+}
+
+__device__ __forceinline__ void fast_two_sum_update(float& hi, float& lo, float inc) {
+  const float s = hi + inc;
+  const float e = (hi - s) + inc;
+  lo = lo + e;
+  hi = s;
+}
+
+// Fold lo back into hi so that |lo| <= ulp(hi)/2 again (Fast2Sum). Between
+// renormalisations |lo| grows by at most ulp(hi)/2 per step, so every 8 steps
+// keeps its own rounding far below the FP32 evaluation error of the RHS.
+__device__ __forceinline__ void renormalise(float& hi, float& lo) {
+  const float s = hi + lo;
+  lo = lo - (s - hi);
+  hi = s;
 }
 
 // (hi + lo) > t for a threshold held as a (hi, lo) pair.
@@ -43,6 +60,7 @@ struct MixedStepper {
   AConsts<double> Cd;
   float cap_hi, cap_lo, esc_hi, esc_lo;
   float h, hh, sixth;
+  unsigned since_renorm = 0;
   bool ready = false;
 
   __device__ __forceinline__ void setup(const TraceLaunch& L) {
@@ -133,8 +151,20 @@ struct MixedStepper {
       finite &= isfinite(inc[i]);
     }
     if (!finite) return STEP_NONFINITE;
+    // Positions move monotonically in t and phi and stay far from 0 in r and
+    // theta relative to one step, so Fast2Sum is exact for them (and for t = 0 or
+    // phi = 0 exactly); momenta cross zero (p^r at periapsis), so TwoSum.
 #pragma unroll
-    for (int i = 0; i < 8; ++i) two_sum_update(hi[i], lo[i], inc[i]);
+    for (int i = 0; i < 4; ++i) {
+      if (K == KIND_ALCUBIERRE || K == KIND_MINKOWSKI) two_sum_update(hi[i], lo[i], inc[i]);
+      else fast_two_sum_update(hi[i], lo[i], inc[i]);
+    }
+#pragma unroll
+    for (int i = 4; i < 8; ++i) two_sum_update(hi[i], lo[i], inc[i]);
+    if ((++since_renorm & 7) == 0) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) renormalise(hi[i], lo[i]);
+    }
     if (L.mixed_flags & MIXED_REPROJECT) {
       float s = 0.0f;
       if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) s = sinf(hi[2]);
@@ -200,19 +230,22 @@ struct MixedStepper {
   __device__ __forceinline__ void finish(const TraceLaunch&) {}
 };
 
-template <int K, int SRC, int SINK>
-__global__ void __launch_bounds__(TRACE_BLOCK) trace_mixed_kernel(const TraceLaunch L) {
+// MINB is the register cap chosen by the autotuner: __launch_bounds__(128, MINB)
+// asks the compiler to fit MINB blocks per SM (1: no cap, ~124 registers;
+// 5: <= 102; 6: <= 85), trading registers for resident warps.
+template <int K, int SRC, int SINK, int MINB>
+__global__ void __launch_bounds__(TRACE_BLOCK, MINB) trace_mixed_kernel(const TraceLaunch L) {
   trace_loop<MixedStepper<K>, K, SRC, SINK>(L);
 }
 
-template <int K, int SRC, int SINK>
-static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
+template <int K, int SRC, int SINK, int MINB>
+static cudaError_t launch_mst_v(const TraceLaunch& L, cudaStream_t s) {
   static int sms = 0, per_sm = 0;
   if (sms == 0) {
     int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_mixed_kernel<K, SRC, SINK>, TRACE_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_mixed_kernel<K, SRC, SINK, MINB>, TRACE_BLOCK, 0);
     per_sm = occ < 1 ? 1 : occ;
   }
   // persistent grid: every resident slot, minus the blocks per SM the caller
@@ -222,8 +255,17 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
   const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
   int grid = (int)(need < slots ? need : slots);
   if (grid < 1) grid = 1;
-  trace_mixed_kernel<K, SRC, SINK><<<grid, TRACE_BLOCK, 0, s>>>(L);
+  trace_mixed_kernel<K, SRC, SINK, MINB><<<grid, TRACE_BLOCK, 0, s>>>(L);
   return cudaGetLastError();
+}
+
+template <int K, int SRC, int SINK>
+static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
+  switch (L.variant) {
+    case 1: return launch_mst_v<K, SRC, SINK, 5>(L, s);
+    case 2: return launch_mst_v<K, SRC, SINK, 6>(L, s);
+    default: return launch_mst_v<K, SRC, SINK, 1>(L, s);
+  }
 }
 
 template <int K>

@@ -56,3 +56,38 @@ def nec_contraction(metric, x, k):
 
 def wec_contraction(metric, x, u):
     return nec_contraction(metric, x, u)
+
+
+def grid(metric, lo, hi, n, t=0.0, nk=16, seed=0x5EED, with_einstein=True, with_k=False):
+    """Einstein tensor and T(k, k) for nk seeded null vectors per point over a
+    regular grid (endpoints included). Returns (points (N, 4), einstein
+    (N, 4, 4) or None, nec (N, nk), k (N, nk, 4) or None)."""
+    g = _ffi.GeonGrid()
+    for i in range(3):
+        g.lo[i] = float(lo[i])
+        g.hi[i] = float(hi[i])
+        g.n[i] = int(n[i])
+    g.t = float(t)
+    npts = int(n[0]) * int(n[1]) * int(n[2])
+    ein = np.empty((npts, 4, 4)) if with_einstein else None
+    nec = np.empty((npts, nk)) if nk else None
+    kk = np.empty((npts, nk, 4)) if (with_k and nk) else None
+    check(_ffi.load().geon_curvature_grid(metric.handle, g, int(nk), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                          dp(ein) if ein is not None else None,
+                                          dp(nec) if nec is not None else None,
+                                          dp(kk) if kk is not None else None))
+    return grid_points(lo, hi, n, t), ein, nec, kk
+
+
+def grid_points(lo, hi, n, t=0.0):
+    """The points of a grid job, in its index order (x fastest)."""
+    axes = []
+    for i in range(3):
+        if int(n[i]) > 1:
+            step = (float(hi[i]) - float(lo[i])) / float(int(n[i]) - 1)
+            axes.append(float(lo[i]) + np.arange(int(n[i]), dtype=np.float64) * step)
+        else:
+            axes.append(np.array([float(lo[i])]))
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    pts = np.stack([np.full(x.size, float(t)), x.ravel(), y.ravel(), z.ravel()], axis=1)
+    return pts

@@ -171,6 +171,18 @@ void geon_set_mixed_reproject(int on);
  * to a sweep), calls made after this keep `blocks_per_sm` resident slots per SM
  * free. Default 0. */
 void geon_set_persistent_reserve(int blocks_per_sm);
+/* Register-cap variant of the mixed kernel per metric kind and ray source
+ * (source 0: camera rays and ray arrays, 1: equatorial shadow rays): 0 = no
+ * cap, 1 = fit 5 blocks of 128 threads per SM, 2 = fit 6. geon_autotune_mixed
+ * times every variant on calibration jobs of this metric (n_rays rays, at most
+ * max_steps each; the equatorial job only for Schwarzschild), selects the
+ * fastest per source and writes ray-steps/s per (source, variant) to
+ * rates_out[6] and the choices to best_out[2] (-1 = source not tuned); either
+ * may be NULL. */
+int geon_set_mixed_variant(int kind, int source, int variant);
+int geon_get_mixed_variant(int kind, int source);
+int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, double* rates_out,
+                        int* best_out);
 
 /* --- curvature.rs ------------------------------------------------------------ */
 int geon_riemann(geon_metric_t m, const double* x, size_t n, double* out);       /* curvature.rs:48, n*256 */
@@ -182,6 +194,25 @@ int geon_stress_energy(geon_metric_t m, const double* x, size_t n, double* out);
  * points when k_shared != 0, else n*nk Vec4 (point-major). out: n*nk. */
 int geon_nec_contraction(geon_metric_t m, const double* x, size_t n, const double* k, size_t nk,
                          int k_shared, double* out);
+/* Curvature over a regular grid (a batch form of curvature.rs with no
+ * counterpart in the reference, which evaluates point by point in
+ * bin/energy_conditions.rs:86-117). Point index p = (iz*ny + iy)*nx + ix at
+ * x = (t, lo[0] + ix*(hi[0]-lo[0])/(nx-1), ...), endpoints included. For each
+ * point: einstein (16 doubles, may be NULL) and nk values of T(k, k) for null
+ * vectors k = e0 + n1 e1 + n2 e2 + n3 e3 in the point's static-observer
+ * Gram-Schmidt tetrad, n uniform on the sphere drawn from the counter-based
+ * stream splitmix64(seed ^ (p*nk + q)); k_out (n*nk*4, may be NULL) returns
+ * the vectors used. */
+typedef struct {
+  double lo[3];
+  double hi[3];
+  int64_t n[3];
+  double t;
+} geon_grid;
+int geon_curvature_grid(geon_metric_t m, const geon_grid* grid, size_t nk, uint64_t seed, double* einstein,
+                        double* nec, double* k_out);
+int geon_curvature_grid_dev(geon_metric_t m, const geon_grid* grid, size_t nk, uint64_t seed,
+                            double* einstein, double* nec, double* k_out, void* stream);
 /* wec_contraction is nec_contraction with a timelike vector (curvature.rs:139-141). */
 int geon_wec_contraction(geon_metric_t m, const double* x, size_t n, const double* u, size_t nu,
                          int u_shared, double* out);
