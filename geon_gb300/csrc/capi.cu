@@ -348,4 +348,563 @@ int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, doub
   return GEON_OK;
 }
 
+
+int geon_get_show_stars(void) { return g_show_stars.load(); }
+
+int geon_metric_create(int kind, const double* params, int nparams, geon_metric_t* out) {
+  if (!out) return fail(GEON_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (kind < GEON_MINKOWSKI || kind > GEON_MORRIS_THORNE) return fail(GEON_ERR_INVALID, "unknown metric kind");
+  if (nparams < 0 || (nparams > 0 && !params)) return fail(GEON_ERR_INVALID, "bad params");
+  MetricDesc d;
+  std::memset(&d, 0, sizeof d);
+  d.kind = kind;
+  // Reference defaults: Schwarzschild::new (schwarzschild.rs:20-28), Alcubierre::default
+  // (alcubierre.rs:21-30), MorrisThorne::default (morris_thorne.rs:15-18).
+  static const double defaults[4][4] = {{0, 0, 0, 0}, {1.0, 1.001, 1000.0, 0}, {2.0, 0.5, 2.0, 0.0}, {1.0, 0, 0, 0}};
+  static const int counts[4] = {0, 3, 4, 1};
+  if (nparams > counts[kind]) return fail(GEON_ERR_INVALID, "too many params for this metric");
+  for (int i = 0; i < 4; ++i) d.p[i] = i < nparams ? params[i] : defaults[kind][i];
+  if (kind == GEON_SCHWARZSCHILD) {
+    d.capture_r = d.p[1] * 2.0 * d.p[0];
+    d.escape_r = d.p[2] * d.p[0];
+  }
+  if (kind == GEON_ALCUBIERRE) {
+    cudaStream_t s = host_stream();
+    DBuf b;
+    GEON_CUDA(b.alloc(sizeof(MetricDesc), s));
+    GEON_CUDA(cudaMemcpyAsync(b.p, &d, sizeof d, cudaMemcpyHostToDevice, s));
+    counted();
+  GEON_CUDA(launch_metric_init(b.as<MetricDesc>(), s));
+    GEON_CUDA(cudaMemcpyAsync(&d, b.p, sizeof d, cudaMemcpyDeviceToHost, s));
+    GEON_CUDA(cudaStreamSynchronize(s));
+  }
+  geon_metric* m = new (std::nothrow) geon_metric;
+  if (!m) return fail(GEON_ERR_OOM, "out of host memory");
+  m->desc = d;
+  *out = m;
+  return GEON_OK;
+}
+
+int geon_metric_destroy(geon_metric_t m) {
+  delete m;
+  return GEON_OK;
+}
+
+int geon_metric_kind(geon_metric_t m) { return m ? m->desc.kind : GEON_ERR_INVALID; }
+
+const char* geon_metric_name(geon_metric_t m) {
+  static const char* names[4] = {"minkowski", "schwarzschild", "alcubierre", "morris_thorne"};
+  return m ? names[m->desc.kind] : "";
+}
+
+static int pointwise(geon_metric_t m, int what, const double* in, size_t n, int in_width, double* out,
+                     int out_width, int32_t* iout) {
+  if (int rc = check_metric(m)) return rc;
+  if (n == 0) return GEON_OK;
+  if (!in || (!out && !iout)) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf din, dout, dflags;
+  GEON_CUDA(din.alloc(sizeof(double) * n * in_width, s));
+  GEON_CUDA(dout.alloc(out ? sizeof(double) * n * out_width : sizeof(int32_t) * n, s));
+  GEON_CUDA(dflags.alloc(sizeof(int), s));
+  GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
+  GEON_CUDA(cudaMemcpyAsync(din.p, in, sizeof(double) * n * in_width, cudaMemcpyHostToDevice, s));
+  counted();
+  GEON_CUDA(launch_pointwise(m->desc, what, din.as<double>(), (int64_t)n, out ? dout.as<double>() : nullptr,
+                             out ? nullptr : dout.as<int32_t>(), dflags.as<int>(), s));
+  if (out) GEON_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double) * n * out_width, cudaMemcpyDeviceToHost, s));
+  else GEON_CUDA(cudaMemcpyAsync(iout, dout.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  int flags = 0;
+  if (int rc = sync_and_flags(s, dflags.as<int>(), &flags)) return rc;
+  return singular_status(flags);
+}
+
+int geon_metric_g(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_G, x, n, 4, out, 16, nullptr); }
+int geon_metric_dg(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_DG, x, n, 4, out, 64, nullptr); }
+int geon_metric_g_inv(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_GINV, x, n, 4, out, 16, nullptr); }
+int geon_metric_christoffel(geon_metric_t m, const double* x, size_t n, double* out) { return pointwise(m, PW_CHRISTOFFEL, x, n, 4, out, 64, nullptr); }
+int geon_metric_terminate(geon_metric_t m, const double* x, size_t n, int32_t* out) { return pointwise(m, PW_TERMINATE, x, n, 4, nullptr, 0, out); }
+int geon_metric_asymptotic_direction(geon_metric_t m, const double* st, size_t n, double* out) { return pointwise(m, PW_ASYM, st, n, 8, out, 3, nullptr); }
+
+int geon_trace_dev(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps, int precision,
+                   int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual,
+                   void* stream) {
+  if (int rc = check_metric(m)) return rc;
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (n == 0) return GEON_OK;
+  if (!y0 || !term || !final_state || !steps_taken || !null_residual)
+    return fail(GEON_ERR_INVALID, "geon_trace_dev needs every device buffer");
+  if (max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DBuf ws;
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) + sizeof(int) * 2, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) + sizeof(int) * 2, s));
+  TraceLaunch L = base_launch(m, step, max_steps);
+  L.n = (int64_t)n;
+  L.y0 = y0;
+  L.term = term;
+  L.yfinal = final_state;
+  L.steps = steps_taken;
+  L.resid = null_residual;
+  L.queue = ws.as<unsigned long long>();
+  L.flags = reinterpret_cast<int*>(L.queue + 1);
+  GEON_CUDA(launch_trace(L, precision, SRC_ARRAY, SINK_TRACE, s));
+  return GEON_OK;
+}
+
+int geon_trace(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps, int precision,
+               int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual) {
+  if (int rc = check_metric(m)) return rc;
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (n == 0) return GEON_OK;
+  if (!y0 || !term) return fail(GEON_ERR_INVALID, "null buffer");
+  if (max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
+  cudaStream_t s = host_stream();
+  DBuf dy0, dterm, dyf, dsteps, dres, ws;
+  GEON_CUDA(dy0.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(dterm.alloc(sizeof(int32_t) * n, s));
+  GEON_CUDA(dyf.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(dsteps.alloc(sizeof(int64_t) * n, s));
+  GEON_CUDA(dres.alloc(sizeof(double) * n, s));
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) + sizeof(int) * 2, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) + sizeof(int) * 2, s));
+  GEON_CUDA(cudaMemcpyAsync(dy0.p, y0, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, s));
+  TraceLaunch L = base_launch(m, step, max_steps);
+  L.n = (int64_t)n;
+  L.y0 = dy0.as<double>();
+  L.term = dterm.as<int32_t>();
+  L.yfinal = dyf.as<double>();
+  L.steps = dsteps.as<int64_t>();
+  L.resid = dres.as<double>();
+  L.queue = ws.as<unsigned long long>();
+  L.flags = reinterpret_cast<int*>(L.queue + 1);
+  GEON_CUDA(launch_trace(L, precision, SRC_ARRAY, SINK_TRACE, s));
+  if (int rc = copy_out(term, dterm.p, sizeof(int32_t) * n, s)) return rc;
+  if (int rc = copy_out(final_state, dyf.p, sizeof(double) * 8 * n, s)) return rc;
+  if (int rc = copy_out(steps_taken, dsteps.p, sizeof(int64_t) * n, s)) return rc;
+  if (int rc = copy_out(null_residual, dres.p, sizeof(double) * n, s)) return rc;
+  int flags = 0;
+  if (int rc = sync_and_flags(s, L.flags, &flags)) return rc;
+  return singular_status(flags);
+}
+
+int geon_camera_tetrad(geon_metric_t m, const double observer[4], double out_tetrad[16]) {
+  if (int rc = check_metric(m)) return rc;
+  if (!observer || !out_tetrad) return fail(GEON_ERR_INVALID, "null buffer");
+  geon_camera cam;
+  std::memset(&cam, 0, sizeof cam);
+  std::memcpy(cam.observer, observer, sizeof cam.observer);
+  cam.fov_y_deg = 60.0;
+  cam.width = cam.height = 1;
+  cam.forward_sign = 1;
+  CameraDesc c;
+  if (int rc = make_camera(m, &cam, 1, c, host_stream())) return rc;
+  std::memcpy(out_tetrad, c.tet, sizeof c.tet);
+  return GEON_OK;
+}
+
+int geon_camera_ray_states(const geon_camera* cam, const double tetrad[16], double du, double dv,
+                           double* out_states) {
+  if (!cam || !tetrad || !out_states || cam->width <= 0 || cam->height <= 0)
+    return fail(GEON_ERR_INVALID, "bad camera arguments");
+  if (cam->forward_sign != 1 && cam->forward_sign != -1) return fail(GEON_ERR_INVALID, "forward_sign must be +1 or -1");
+  CameraDesc c;
+  std::memcpy(c.tet, tetrad, sizeof c.tet);
+  std::memcpy(c.obs, cam->observer, sizeof c.obs);
+  const double fov = cam->fov_y_deg * RADS_PER_DEG;
+  const double aspect = (double)cam->width / (double)cam->height;
+  c.h_img = std::tan(fov * 0.5);
+  c.w_img = c.h_img * aspect;
+  c.width_d = (double)cam->width;
+  c.height_d = (double)cam->height;
+  c.width = cam->width;
+  c.height = cam->height;
+  c.spa = 1;
+  c.inv_spa = 1.0;
+  c.forward_sign = cam->forward_sign;
+  const size_t n = (size_t)(cam->width * cam->height);
+  cudaStream_t s = host_stream();
+  DBuf d;
+  GEON_CUDA(d.alloc(sizeof(double) * 8 * n, s));
+  counted();
+  GEON_CUDA(launch_camera_rays(c, du, dv, d.as<double>(), s));
+  GEON_CUDA(cudaMemcpyAsync(out_states, d.p, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
+                   geon_render_stats* stats, int32_t* pixel_class, int64_t* pixel_steps) {
+  if (int rc = check_metric(m)) return rc;
+  if (!cfg || !rgb) return fail(GEON_ERR_INVALID, "null buffer");
+  if (!valid_precision(cfg->precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (cfg->max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
+  cudaStream_t s = host_stream();
+  const int64_t spa = cfg->samples_per_axis < 1 ? 1 : cfg->samples_per_axis;
+  CameraDesc c;
+  if (int rc = make_camera(m, cam, spa, c, s)) return rc;
+  const int64_t npix = cam->width * cam->height;
+  const int64_t nsamp = npix * spa * spa;
+  DBuf dsrgb, dterm, dsteps, dres, drgb, dcls, dpst, ws;
+  GEON_CUDA(dsrgb.alloc(sizeof(float) * 3 * nsamp, s));
+  GEON_CUDA(dterm.alloc(sizeof(int32_t) * nsamp, s));
+  GEON_CUDA(dsteps.alloc(sizeof(int64_t) * nsamp, s));
+  GEON_CUDA(dres.alloc(sizeof(double) * nsamp, s));
+  GEON_CUDA(drgb.alloc(sizeof(float) * 3 * npix, s));
+  GEON_CUDA(dcls.alloc(sizeof(int32_t) * npix, s));
+  GEON_CUDA(dpst.alloc(sizeof(int64_t) * npix, s));
+  const size_t ws_bytes = sizeof(unsigned long long) * 8;
+  GEON_CUDA(ws.alloc(ws_bytes, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, ws_bytes, s));
+  TraceLaunch L = base_launch(m, cfg->step, cfg->max_steps);
+  L.cam = c;
+  L.n = nsamp;
+  L.term = dterm.as<int32_t>();
+  L.steps = dsteps.as<int64_t>();
+  L.resid = dres.as<double>();
+  L.srgb = dsrgb.as<float>();
+  L.show_stars = cfg->show_stars < 0 ? g_show_stars.load() : (cfg->show_stars != 0);
+  for (int q = 0; q < 3; ++q) {
+    L.captured_rgb[q] = cfg->captured_rgb[q];
+    L.diverged_rgb[q] = cfg->diverged_rgb[q];
+  }
+  unsigned long long* wsu = ws.as<unsigned long long>();
+  L.queue = wsu;
+  L.flags = reinterpret_cast<int*>(wsu + 1);
+  unsigned long long* dstats = wsu + 2;  // 6 counters
+  GEON_CUDA(launch_trace(L, cfg->precision, SRC_CAMERA, SINK_RENDER, s));
+  counted();
+  GEON_CUDA(launch_render_reduce(dsrgb.as<float>(), dterm.as<int32_t>(), dsteps.as<int64_t>(),
+                                 dres.as<double>(), npix, spa, drgb.as<float>(), dcls.as<int32_t>(),
+                                 dpst.as<int64_t>(), dstats, s));
+  unsigned long long hst[6];
+  GEON_CUDA(cudaMemcpyAsync(rgb, drgb.p, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, s));
+  if (int rc = copy_out(pixel_class, dcls.p, sizeof(int32_t) * npix, s)) return rc;
+  if (int rc = copy_out(pixel_steps, dpst.p, sizeof(int64_t) * npix, s)) return rc;
+  GEON_CUDA(cudaMemcpyAsync(hst, dstats, sizeof hst, cudaMemcpyDeviceToHost, s));
+  int flags = 0;
+  if (int rc = sync_and_flags(s, L.flags, &flags)) return rc;
+  if (stats) {
+    stats->captured = (int64_t)hst[0];
+    stats->escaped = (int64_t)hst[1];
+    stats->diverged = (int64_t)hst[2];
+    double mr;
+    std::memcpy(&mr, &hst[4], sizeof mr);
+    stats->max_null_residual = mr;
+    stats->avg_steps = (double)(int64_t)hst[3] / (double)npix;
+    stats->total_steps = (int64_t)hst[5];
+  }
+  return singular_status(flags);
+}
+
+int geon_render(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
+                geon_render_stats* stats) {
+  return geon_render_ex(m, cam, cfg, rgb, stats, nullptr, nullptr);
+}
+
+int geon_sky_sample(const double* dir, size_t n, int show_stars, float* rgb) {
+  if (n == 0) return GEON_OK;
+  if (!dir || !rgb) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf dd, dr;
+  GEON_CUDA(dd.alloc(sizeof(double) * 3 * n, s));
+  GEON_CUDA(dr.alloc(sizeof(float) * 3 * n, s));
+  GEON_CUDA(cudaMemcpyAsync(dd.p, dir, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  counted();
+  GEON_CUDA(launch_sky(dd.as<double>(), (int64_t)n, show_stars, dr.as<float>(), s));
+  GEON_CUDA(cudaMemcpyAsync(rgb, dr.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+static int curvature_call(geon_metric_t m, int what, const double* x, size_t n, const double* k, size_t nk,
+                          int k_shared, double* out, int out_width) {
+  if (int rc = check_metric(m)) return rc;
+  if (n == 0) return GEON_OK;
+  if (!x || !out) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf dx, dk, dout, dflags;
+  const size_t kcount = what == 5 ? (k_shared ? nk : nk * n) : 0;
+  GEON_CUDA(dx.alloc(sizeof(double) * 4 * n, s));
+  GEON_CUDA(dk.alloc(sizeof(double) * 4 * kcount, s));
+  GEON_CUDA(dout.alloc(sizeof(double) * n * out_width, s));
+  GEON_CUDA(dflags.alloc(sizeof(int), s));
+  GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
+  GEON_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, s));
+  if (kcount) GEON_CUDA(cudaMemcpyAsync(dk.p, k, sizeof(double) * 4 * kcount, cudaMemcpyHostToDevice, s));
+  counted();
+  GEON_CUDA(launch_curvature(m->desc, what, dx.as<double>(), (int64_t)n, dk.as<double>(), (int64_t)nk,
+                             k_shared, dout.as<double>(), dflags.as<int>(), s));
+  GEON_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double) * n * out_width, cudaMemcpyDeviceToHost, s));
+  int flags = 0;
+  if (int rc = sync_and_flags(s, dflags.as<int>(), &flags)) return rc;
+  return singular_status(flags);
+}
+
+int geon_riemann(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 0, x, n, nullptr, 0, 1, out, 256); }
+int geon_ricci(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 1, x, n, nullptr, 0, 1, out, 16); }
+int geon_ricci_scalar(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 2, x, n, nullptr, 0, 1, out, 1); }
+int geon_einstein(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 3, x, n, nullptr, 0, 1, out, 16); }
+int geon_stress_energy(geon_metric_t m, const double* x, size_t n, double* out) { return curvature_call(m, 4, x, n, nullptr, 0, 1, out, 16); }
+
+int geon_nec_contraction(geon_metric_t m, const double* x, size_t n, const double* k, size_t nk, int k_shared,
+                         double* out) {
+  if (nk == 0 || n == 0) return GEON_OK;
+  if (!k) return fail(GEON_ERR_INVALID, "null k");
+  return curvature_call(m, 5, x, n, k, nk, k_shared, out, (int)nk);
+}
+
+int geon_wec_contraction(geon_metric_t m, const double* x, size_t n, const double* u, size_t nu, int u_shared,
+                         double* out) {
+  return geon_nec_contraction(m, x, n, u, nu, u_shared, out);
+}
+
+int geon_equatorial_rays(geon_metric_t m, double r_obs, const double* alpha, size_t n, double* out_states) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "equatorial rays need a Schwarzschild metric");
+  if (n == 0) return GEON_OK;
+  if (!alpha || !out_states) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf da, dout;
+  GEON_CUDA(da.alloc(sizeof(double) * n, s));
+  GEON_CUDA(dout.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(cudaMemcpyAsync(da.p, alpha, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  counted();
+  GEON_CUDA(launch_equatorial_rays(m->desc.p[0], r_obs, da.as<double>(), (int64_t)n, dout.as<double>(), s));
+  GEON_CUDA(cudaMemcpyAsync(out_states, dout.p, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+// Classify rays launched at the given angles on stream s (device buffers).
+static int classify_dev(geon_metric_t m, double r_obs, const double* d_alpha, int64_t n, double step,
+                        int64_t max_steps, int precision, int32_t* d_term, int64_t* d_steps,
+                        cudaStream_t s) {
+  DBuf ws;
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 2, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 2, s));
+  TraceLaunch L = base_launch(m, step, max_steps);
+  L.n = n;
+  L.alpha = d_alpha;
+  L.r_obs = r_obs;
+  L.term = d_term;
+  L.steps = d_steps;
+  L.queue = ws.as<unsigned long long>();
+  L.flags = reinterpret_cast<int*>(L.queue + 1);
+  GEON_CUDA(launch_trace(L, precision, SRC_EQUATORIAL, SINK_SHADOW, s));
+  return GEON_OK;
+}
+
+int geon_shadow_classify(geon_metric_t m, double r_obs, const double* alpha, size_t n, double step,
+                         int64_t max_steps, int precision, int32_t* term, int64_t* steps) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow classification needs a Schwarzschild metric");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (n == 0) return GEON_OK;
+  if (!alpha || !term) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf da, dt, dst;
+  GEON_CUDA(da.alloc(sizeof(double) * n, s));
+  GEON_CUDA(dt.alloc(sizeof(int32_t) * n, s));
+  GEON_CUDA(dst.alloc(sizeof(int64_t) * n, s));
+  GEON_CUDA(cudaMemcpyAsync(da.p, alpha, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (int rc = classify_dev(m, r_obs, da.as<double>(), (int64_t)n, step, max_steps, precision,
+                            dt.as<int32_t>(), dst.as<int64_t>(), s))
+    return rc;
+  GEON_CUDA(cudaMemcpyAsync(term, dt.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  if (int rc = copy_out(steps, dst.p, sizeof(int64_t) * n, s)) return rc;
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+// Bisection of bin/validate_shadow.rs:70-79, evaluated L levels at a time: for
+// each bracket every midpoint the next L sequential halvings could visit (a
+// complete binary tree of 2^L - 1 launch angles, built on the device with the
+// same 0.5*(lo+hi) arithmetic) is traced in one launch, then a walk kernel
+// replays the sequential path through the tree. The result equals the
+// sequential loop bit for bit, with ceil(iters / L) dependent rounds instead of
+// iters, and no host round trip between rounds (3 launches per round).
+
+int geon_shadow_bisect_dev(geon_metric_t m, double r_obs, const double* lo, const double* hi, size_t nb,
+                           int iters, double step, int64_t max_steps, int precision, double* alpha_c,
+                           double* lo_out, double* hi_out, int64_t* steps_out, void* stream) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow bisection needs a Schwarzschild metric");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (nb == 0) return GEON_OK;
+  if (!lo || !hi || !alpha_c || iters < 0 || max_steps < 0) return fail(GEON_ERR_INVALID, "bad bisection arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int Lmax = (int)bisect_levels(nb);
+  const int64_t cap = (int64_t)nb * ((1LL << Lmax) - 1);
+  DBuf work, tree, tterm, tsteps, ws;
+  GEON_CUDA(work.alloc(sizeof(double) * 2 * nb + sizeof(int64_t) * nb, s));
+  GEON_CUDA(tree.alloc(sizeof(double) * cap, s));
+  GEON_CUDA(tterm.alloc(sizeof(int32_t) * cap, s));
+  GEON_CUDA(tsteps.alloc(sizeof(int64_t) * cap, s));
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 2, s));
+  double* wlo = work.as<double>();
+  double* whi = wlo + nb;
+  int64_t* wst = reinterpret_cast<int64_t*>(whi + nb);
+  GEON_CUDA(cudaMemcpyAsync(wlo, lo, sizeof(double) * nb, cudaMemcpyDefault, s));
+  GEON_CUDA(cudaMemcpyAsync(whi, hi, sizeof(double) * nb, cudaMemcpyDefault, s));
+  GEON_CUDA(cudaMemsetAsync(wst, 0, sizeof(int64_t) * nb, s));
+  int remaining = iters;
+  while (remaining > 0) {
+    const int L = remaining < Lmax ? remaining : Lmax;
+    const int64_t per = (1LL << L) - 1;
+    const int64_t nr = (int64_t)nb * per;
+    counted();
+    GEON_CUDA(launch_bisect_build((int64_t)nb, per, wlo, whi, tree.as<double>(), s));
+    GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 2, s));
+    TraceLaunch T = base_launch(m, step, max_steps);
+    T.n = nr;
+    T.alpha = tree.as<double>();
+    T.r_obs = r_obs;
+    T.term = tterm.as<int32_t>();
+    T.steps = tsteps.as<int64_t>();
+    T.queue = ws.as<unsigned long long>();
+    T.flags = reinterpret_cast<int*>(T.queue + 1);
+    GEON_CUDA(launch_trace(T, precision, SRC_EQUATORIAL, SINK_SHADOW, s));
+    counted();
+    GEON_CUDA(launch_bisect_walk((int64_t)nb, per, L, tree.as<double>(), tterm.as<int32_t>(),
+                                 tsteps.as<int64_t>(), wlo, whi, wst, s));
+    remaining -= L;
+  }
+  counted();
+  GEON_CUDA(launch_bisect_finish((int64_t)nb, wlo, whi, alpha_c, s));
+  if (lo_out) GEON_CUDA(cudaMemcpyAsync(lo_out, wlo, sizeof(double) * nb, cudaMemcpyDefault, s));
+  if (hi_out) GEON_CUDA(cudaMemcpyAsync(hi_out, whi, sizeof(double) * nb, cudaMemcpyDefault, s));
+  if (steps_out) GEON_CUDA(cudaMemcpyAsync(steps_out, wst, sizeof(int64_t) * nb, cudaMemcpyDefault, s));
+  return GEON_OK;
+}
+
+int geon_shadow_bisect(geon_metric_t m, double r_obs, const double* lo, const double* hi, size_t nb, int iters,
+                       double step, int64_t max_steps, int precision, double* alpha_c, double* lo_out,
+                       double* hi_out, int64_t* steps_out) {
+  if (int rc = check_metric(m)) return rc;
+  if (nb == 0) return GEON_OK;
+  if (!lo || !hi || !alpha_c) return fail(GEON_ERR_INVALID, "bad bisection arguments");
+  cudaStream_t s = host_stream();
+  DBuf io;
+  GEON_CUDA(io.alloc(sizeof(double) * 5 * nb + sizeof(int64_t) * nb, s));
+  double* d_lo = io.as<double>();
+  double* d_hi = d_lo + nb;
+  double* d_ac = d_hi + nb;
+  double* d_lo_o = d_ac + nb;
+  double* d_hi_o = d_lo_o + nb;
+  int64_t* d_st = reinterpret_cast<int64_t*>(d_hi_o + nb);
+  GEON_CUDA(cudaMemcpyAsync(d_lo, lo, sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(cudaMemcpyAsync(d_hi, hi, sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+  if (int rc = geon_shadow_bisect_dev(m, r_obs, d_lo, d_hi, nb, iters, step, max_steps, precision, d_ac, d_lo_o,
+                                      d_hi_o, d_st, s))
+    return rc;
+  GEON_CUDA(cudaMemcpyAsync(alpha_c, d_ac, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
+  if (int rc = copy_out(lo_out, d_lo_o, sizeof(double) * nb, s)) return rc;
+  if (int rc = copy_out(hi_out, d_hi_o, sizeof(double) * nb, s)) return rc;
+  if (int rc = copy_out(steps_out, d_st, sizeof(int64_t) * nb, s)) return rc;
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+int geon_shadow_classify_dev(geon_metric_t m, double r_obs, const double* alpha, size_t n, double step,
+                             int64_t max_steps, int precision, int32_t* term, int64_t* steps, void* stream) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "shadow classification needs a Schwarzschild metric");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (n == 0) return GEON_OK;
+  if (!alpha || !term) return fail(GEON_ERR_INVALID, "null buffer");
+  return classify_dev(m, r_obs, alpha, (int64_t)n, step, max_steps, precision, term, steps,
+                      static_cast<cudaStream_t>(stream));
+}
+
+unsigned long long geon_launch_count(void) { return g_launches.load(); }
+
+
+int geon_probe_fma_peak(int fp64, double* tflops) {
+  if (!tflops) return fail(GEON_ERR_INVALID, "null output");
+  int dev = 0, sms = 0;
+  GEON_CUDA(cudaGetDevice(&dev));
+  GEON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256;
+  const int iters = fp64 ? 4096 : 65536;
+  cudaStream_t s = host_stream();
+  DBuf out;
+  GEON_CUDA(out.alloc((size_t)blocks * threads * 8, s));
+  cudaEvent_t a, b;
+  GEON_CUDA(cudaEventCreate(&a));
+  GEON_CUDA(cudaEventCreate(&b));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    GEON_CUDA(cudaEventRecord(a, s));
+    counted();
+    GEON_CUDA(launch_fma_probe(fp64, out.p, blocks, threads, iters, s));
+    GEON_CUDA(cudaEventRecord(b, s));
+    GEON_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    GEON_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (rep > 0 && ms < best) best = ms;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return GEON_OK;
+}
+
+
+static int grid_desc(const geon_grid* g, GridDesc& d, int64_t& n) {
+  if (!g || g->n[0] < 1 || g->n[1] < 1 || g->n[2] < 1) return fail(GEON_ERR_INVALID, "bad grid");
+  std::memcpy(d.lo, g->lo, sizeof d.lo);
+  std::memcpy(d.hi, g->hi, sizeof d.hi);
+  std::memcpy(d.n, g->n, sizeof d.n);
+  d.t = g->t;
+  n = g->n[0] * g->n[1] * g->n[2];
+  return GEON_OK;
+}
+
+int geon_curvature_grid_dev(geon_metric_t m, const geon_grid* grid, size_t nk, uint64_t seed, double* einstein,
+                            double* nec, double* k_out, void* stream) {
+  if (int rc = check_metric(m)) return rc;
+  GridDesc d;
+  int64_t n = 0;
+  if (int rc = grid_desc(grid, d, n)) return rc;
+  if (nk > 0 && !nec) return fail(GEON_ERR_INVALID, "nec output needed when nk > 0");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DBuf dflags;
+  GEON_CUDA(dflags.alloc(sizeof(int), s));
+  GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
+  counted();
+  GEON_CUDA(launch_curvature_grid(m->desc, d, (int64_t)nk, seed, einstein, nec, k_out, dflags.as<int>(), s));
+  return GEON_OK;
+}
+
+int geon_curvature_grid(geon_metric_t m, const geon_grid* grid, size_t nk, uint64_t seed, double* einstein,
+                        double* nec, double* k_out) {
+  if (int rc = check_metric(m)) return rc;
+  GridDesc d;
+  int64_t n = 0;
+  if (int rc = grid_desc(grid, d, n)) return rc;
+  if (nk > 0 && !nec) return fail(GEON_ERR_INVALID, "nec output needed when nk > 0");
+  cudaStream_t s = host_stream();
+  DBuf de, dn, dk, dflags;
+  if (einstein) GEON_CUDA(de.alloc(sizeof(double) * 16 * n, s));
+  if (nk) GEON_CUDA(dn.alloc(sizeof(double) * nk * n, s));
+  if (k_out && nk) GEON_CUDA(dk.alloc(sizeof(double) * 4 * nk * n, s));
+  GEON_CUDA(dflags.alloc(sizeof(int), s));
+  GEON_CUDA(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
+  counted();
+  GEON_CUDA(launch_curvature_grid(m->desc, d, (int64_t)nk, seed, einstein ? de.as<double>() : nullptr,
+                                  nk ? dn.as<double>() : nullptr, (k_out && nk) ? dk.as<double>() : nullptr,
+                                  dflags.as<int>(), s));
+  if (int rc = copy_out(einstein, de.p, sizeof(double) * 16 * n, s)) return rc;
+  if (nk) {
+    if (int rc = copy_out(nec, dn.p, sizeof(double) * nk * n, s)) return rc;
+    if (int rc = copy_out(k_out, dk.p, sizeof(double) * 4 * nk * n, s)) return rc;
+  }
+  int flags = 0;
+  if (int rc = sync_and_flags(s, dflags.as<int>(), &flags)) return rc;
+  return singular_status(flags);
+}
+
 }  // extern "C"
