@@ -19,6 +19,13 @@ namespace geon {
 
 constexpr double FD_H = 1e-5;  // Metric::fd_step default (metric/mod.rs:73-75)
 
+// x + 0.0 (the first addition of a sum that starts at +0.0) without spending an
+// FP64 instruction: only -0.0 changes (to +0.0).
+__device__ __forceinline__ double plus_zero(double x) {
+  const long long b = __double_as_longlong(x);
+  return b == (long long)0x8000000000000000ULL ? 0.0 : x;
+}
+
 // types.rs:22-30
 __device__ __forceinline__ double dot4(const double g[16], const double a[4], const double b[4]) {
   double s = 0.0;
@@ -77,6 +84,33 @@ __device__ __forceinline__ bool inv4(const double a[16], double out[16]) {
 }
 
 // ---------------------------------------------------------------------------
+// The varying entries of g for the metrics whose Christoffel symbols use the
+// finite-difference fallback. metric_g and the sparse Christoffel code both
+// call these, so both see the same bits.
+// ---------------------------------------------------------------------------
+// alcubierre.rs:33-63: g_tt = -1 + v^2 f^2, g_tx = g_xt = -v f
+__device__ __forceinline__ void alc_g00_g01(const MetricDesc& M, const double x[4], double* g00, double* g01) {
+  const double R = M.p[0], s = M.p[1], v = M.p[2], ship_x = M.p[3];
+  const double dx = x[1] - ship_x, dy = x[2], dz = x[3];
+  const double r_s = sqrt(dx * dx + dy * dy + dz * dz);
+  const double t_plus = dm::tanh_det((r_s + R) / s);
+  const double t_minus = dm::tanh_det((r_s - R) / s);
+  const double f = (t_plus - t_minus) / M.alc_denom;
+  *g00 = -1.0 + v * v * f * f;
+  *g01 = -v * f;
+}
+
+// morris_thorne.rs:22-36: g_thth = b0^2 + l^2, g_phph = (b0^2 + l^2) sin^2(theta)
+__device__ __forceinline__ void mt_g22_g33(const MetricDesc& M, const double x[4], double* g22, double* g33) {
+  const double l = x[1], theta = x[2], b0 = M.p[0];
+  const double r2 = b0 * b0 + l * l;
+  double sin_t, cos_t;
+  dm::sincos_det(theta, &sin_t, &cos_t);
+  *g22 = r2;
+  *g33 = r2 * sin_t * sin_t;
+}
+
+// ---------------------------------------------------------------------------
 // g(x) for each metric (dense 4x4, row-major)
 // ---------------------------------------------------------------------------
 template <int K>
@@ -95,27 +129,21 @@ __device__ __forceinline__ void metric_g(const MetricDesc& M, const double x[4],
     g[10] = r * r;
     g[15] = r * r * sin_t * sin_t;
   } else if (K == KIND_ALCUBIERRE) {  // alcubierre.rs:33-63
-    const double R = M.p[0], s = M.p[1], v = M.p[2], ship_x = M.p[3];
-    const double dx = x[1] - ship_x, dy = x[2], dz = x[3];
-    const double r_s = sqrt(dx * dx + dy * dy + dz * dz);
-    const double t_plus = dm::tanh_det((r_s + R) / s);
-    const double t_minus = dm::tanh_det((r_s - R) / s);
-    const double f = (t_plus - t_minus) / M.alc_denom;
-    g[0] = -1.0 + v * v * f * f;
-    g[1] = -v * f;
-    g[4] = -v * f;
+    double g00, g01;
+    alc_g00_g01(M, x, &g00, &g01);
+    g[0] = g00;
+    g[1] = g01;
+    g[4] = g01;
     g[5] = 1.0;
     g[10] = 1.0;
     g[15] = 1.0;
   } else {  // morris_thorne.rs:22-36
-    const double l = x[1], theta = x[2], b0 = M.p[0];
-    const double r2 = b0 * b0 + l * l;
-    double sin_t, cos_t;
-    dm::sincos_det(theta, &sin_t, &cos_t);
+    double g22, g33;
+    mt_g22_g33(M, x, &g22, &g33);
     g[0] = -1.0;
     g[5] = 1.0;
-    g[10] = r2;
-    g[15] = r2 * sin_t * sin_t;
+    g[10] = g22;
+    g[15] = g33;
   }
 }
 
@@ -222,6 +250,13 @@ __device__ __forceinline__ bool christoffel_generic(const MetricDesc& M, const d
   return ok;
 }
 
+// Generated: the sparse finite-difference Christoffel symbols and geodesic
+// right-hand sides of Alcubierre and Morris-Thorne (in this namespace).
+#include "christoffel_sparse.cuh"
+
+// Christoffel symbols: analytic for Minkowski and Schwarzschild (their
+// overrides), the finite-difference fallback for the others, evaluated by the
+// generated sparse code (same bits as christoffel_generic).
 template <int K>
 __device__ __forceinline__ bool metric_christoffel(const MetricDesc& M, const double x[4], double G[64]) {
   if (K == KIND_MINKOWSKI) {
@@ -231,8 +266,10 @@ __device__ __forceinline__ bool metric_christoffel(const MetricDesc& M, const do
   } else if (K == KIND_SCHWARZSCHILD) {
     christoffel_schw(M, x, G);
     return true;
+  } else if (K == KIND_ALCUBIERRE) {
+    return christoffel_alcubierre_sparse(M, x, G);
   } else {
-    return christoffel_generic<K>(M, x, G);
+    return christoffel_morris_thorne_sparse(M, x, G);
   }
 }
 
@@ -293,12 +330,6 @@ __device__ __forceinline__ void metric_asymptotic_direction(const double x[4], c
   }
 }
 
-// x + 0.0 (the first addition of a sum that starts at +0.0) without spending an
-// FP64 instruction: only -0.0 changes (to +0.0).
-__device__ __forceinline__ double plus_zero(double x) {
-  const long long b = __double_as_longlong(x);
-  return b == (long long)0x8000000000000000ULL ? 0.0 : x;
-}
 
 // ---------------------------------------------------------------------------
 // Geodesic right-hand side (geodesic.rs:38-59): k = (p, -Gamma^mu_ab p^a p^b).
@@ -348,19 +379,10 @@ __device__ __forceinline__ bool geodesic_rhs(const MetricDesc& M, const double y
     s += cot * p3 * p2;
     k[7] = -s;
     return true;
+  } else if (K == KIND_ALCUBIERRE) {
+    return rhs_alcubierre_sparse(M, y, k);
   } else {
-    double G[64];
-    const bool ok = christoffel_generic<K>(M, y, G);
-#pragma unroll
-    for (int mu = 0; mu < 4; ++mu) {
-      double s = 0.0;
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) s += G[16 * mu + 4 * a + b] * y[4 + a] * y[4 + b];
-      k[4 + mu] = -s;
-    }
-    return ok;
+    return rhs_morris_thorne_sparse(M, y, k);
   }
 }
 

@@ -34,7 +34,11 @@ def test_grid_morris_thorne_throat_energy_density(geon):
     assert abs(at0 - (-1.0 / (8.0 * np.pi))) < 1e-6
     mid = np.argmin(np.abs(pts[:, 1]))
     assert abs(t_tt[mid] - (-1.0 / (8.0 * np.pi))) < 1e-4
-    assert np.all(nec[np.abs(pts[:, 1]) < 0.5] < 0)  # NEC violated near the throat
+    # NEC: violated by every throat point for some null direction (the radial
+    # ones: rho + p_r < 0) and never clearly satisfied (tangential: rho + p_t = 0)
+    near = np.abs(pts[:, 1]) < 0.5
+    assert np.all(nec[near].min(axis=1) < -1e-3)
+    assert np.all(nec[near] < 1e-6)  # rho + p_t = 0 up to the ~1e-7 FD noise of T
 
 
 def test_grid_schwarzschild_vacuum(geon):
