@@ -54,6 +54,32 @@ class GeonRenderStats(ctypes.Structure):
                 ("avg_steps", ctypes.c_double), ("total_steps", ctypes.c_int64)]
 
 
+class GeonJob(ctypes.Structure):
+    """geon_job: one serving request (pointers are plain addresses)."""
+    _fields_ = [("type", ctypes.c_int32), ("metric_kind", ctypes.c_int32),
+                ("metric_params", ctypes.c_double * 4), ("nparams", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("deadline_s", ctypes.c_double),
+                ("camera", GeonCamera), ("render", GeonRenderConfig),
+                ("rgb", c_void_p), ("render_stats", c_void_p), ("pixel_class", c_void_p),
+                ("pixel_steps", c_void_p),
+                ("r_obs", ctypes.c_double), ("lo", ctypes.c_double), ("hi", ctypes.c_double),
+                ("step", ctypes.c_double), ("max_steps", ctypes.c_int64), ("iters", ctypes.c_int32),
+                ("rays_per_round", ctypes.c_int32), ("alpha_c", c_void_p), ("lo_out", c_void_p),
+                ("hi_out", c_void_p), ("steps_out", c_void_p),
+                ("grid", GeonGrid), ("nk", ctypes.c_int64), ("seed", ctypes.c_uint64),
+                ("einstein", c_void_p), ("nec", c_void_p)]
+
+
+class GeonServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("queued", ctypes.c_int64), ("running", ctypes.c_int64),
+                ("completed_by_type", ctypes.c_int64 * 3),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("p50_ms_by_type", ctypes.c_double * 3), ("p99_ms_by_type", ctypes.c_double * 3),
+                ("ray_steps", ctypes.c_double), ("grid_points", ctypes.c_double), ("wall_s", ctypes.c_double),
+                ("epochs", ctypes.c_int64)]
+
+
 # name -> (restype, argtypes); every exported symbol of include/geon_gpu.h
 SIGNATURES = {
     "geon_version": (ctypes.c_char_p, []),
@@ -118,6 +144,14 @@ SIGNATURES = {
     "geon_shadow_bisect_dev_noalloc": (ctypes.c_int, [c_void_p, ctypes.c_double, c_void_p, c_void_p, c_size_t,
                                                       ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
                                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "geon_server_create": (ctypes.c_int, [c_size_t, ctypes.POINTER(c_void_p)]),
+    "geon_server_submit": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonJob), ctypes.POINTER(ctypes.c_uint64)]),
+    "geon_server_poll": (ctypes.c_int, [c_void_p, ctypes.c_uint64]),
+    "geon_server_wait": (ctypes.c_int, [c_void_p, ctypes.c_uint64, ctypes.c_double]),
+    "geon_server_wait_all": (ctypes.c_int, [c_void_p, ctypes.c_double]),
+    "geon_server_cancel": (ctypes.c_int, [c_void_p, ctypes.c_uint64]),
+    "geon_server_stats_get": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonServerStats)]),
+    "geon_server_destroy": (ctypes.c_int, [c_void_p]),
     "geon_launch_count": (ctypes.c_ulonglong, []),
     "geon_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, c_double_p]),
 }

@@ -28,6 +28,7 @@ UNITS = [
     ("curvature_fp64.cu", ["--fmad=false"]),
     ("capi.cu", ["--fmad=false"]),
     ("noalloc.cu", ["--fmad=false"]),
+    ("serve.cu", ["--fmad=false"]),
 ]
 
 

@@ -181,6 +181,9 @@ cudaError_t launch_trace_any(const TraceLaunch& L, int precision, int src, int s
 void note_launches(unsigned long long n) { counted(n); }
 int set_last_error(int code, const char* msg) { return fail(code, msg); }
 int bisect_levels_for(size_t nb) { return (int)bisect_levels(nb); }
+int camera_desc_for(geon_metric_t m, const geon_camera* cam, int64_t spa, CameraDesc& c, cudaStream_t s) {
+  return make_camera(m, cam, spa, c, s);
+}
 }  // namespace geon
 
 // Kernels defined in trace_fp64.cu used only from here.

@@ -122,6 +122,7 @@ cudaError_t launch_trace_any(const TraceLaunch& L, int precision, int src, int s
 void note_launches(unsigned long long n);
 int set_last_error(int code, const char* msg);
 int bisect_levels_for(size_t nb);
+int camera_desc_for(geon_metric_t m, const geon_camera* cam, int64_t spa, CameraDesc& c, cudaStream_t s);
 
 // pointwise "what" codes
 enum : int { PW_G = 0, PW_DG = 1, PW_GINV = 2, PW_CHRISTOFFEL = 3, PW_TERMINATE = 4, PW_ASYM = 5 };

@@ -7,6 +7,7 @@
 
 #include "internal.h"
 #include "metric_fp64.cuh"
+#include "serve_common.cuh"
 #include "trace_common.cuh"
 
 namespace geon {
@@ -41,11 +42,80 @@ struct Fp64Stepper {
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
   }
+  // Serving: a lane's ray state as 16 words, and its restoration.
+  __device__ __forceinline__ void save(uint32_t w[16]) const {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(y[i]);
+      w[2 * i] = (uint32_t)b;
+      w[2 * i + 1] = (uint32_t)(b >> 32);
+    }
+  }
+  __device__ __forceinline__ void restore(const TraceLaunch&, const uint32_t w[16], int64_t) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      y[i] = __longlong_as_double((long long)(((unsigned long long)w[2 * i + 1] << 32) | w[2 * i]));
+  }
+  __device__ __forceinline__ void rebind(const TraceLaunch&) {}
 };
 
 template <int K, int SRC, int SINK>
 __global__ void __launch_bounds__(TRACE_BLOCK) trace_fp64_kernel(const TraceLaunch L) {
   trace_loop<Fp64Stepper<K>, K, SRC, SINK>(L);
+}
+
+// Serving engine kernel for the FP64 classes (serve_common.cuh).
+template <int K>
+__global__ void __launch_bounds__(TRACE_BLOCK) serve_fp64_kernel(const ServeJob* jobs, ServeCounters cnt,
+                                                                  ServeClass* cl, const unsigned* epoch, int budget) {
+  serve_loop<Fp64Stepper<K>, K>(jobs, cnt, cl, epoch, budget);
+}
+
+template <int K>
+static cudaError_t launch_serve_fp64_k(const ServeJob* jobs, ServeCounters cnt, ServeClass* cl, const unsigned* epoch,
+                                       int budget, int blocks, cudaStream_t s) {
+  serve_fp64_kernel<K><<<blocks, TRACE_BLOCK, 0, s>>>(jobs, cnt, cl, epoch, budget);
+  return cudaGetLastError();
+}
+
+int serve_fp64_blocks_per_sm(int kind) {
+  int occ = 0;
+  switch (kind) {
+    case KIND_MINKOWSKI: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_fp64_kernel<KIND_MINKOWSKI>, TRACE_BLOCK, 0); break;
+    case KIND_SCHWARZSCHILD: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_fp64_kernel<KIND_SCHWARZSCHILD>, TRACE_BLOCK, 0); break;
+    case KIND_ALCUBIERRE: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_fp64_kernel<KIND_ALCUBIERRE>, TRACE_BLOCK, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_fp64_kernel<KIND_MORRIS_THORNE>, TRACE_BLOCK, 0); break;
+  }
+  return occ < 1 ? 1 : occ;
+}
+
+cudaError_t launch_serve_fp64(int kind, const ServeJob* jobs, ServeCounters cnt, ServeClass* cl,
+                              const unsigned* epoch, int budget, int blocks, cudaStream_t s) {
+  switch (kind) {
+    case KIND_MINKOWSKI: return launch_serve_fp64_k<KIND_MINKOWSKI>(jobs, cnt, cl, epoch, budget, blocks, s);
+    case KIND_SCHWARZSCHILD: return launch_serve_fp64_k<KIND_SCHWARZSCHILD>(jobs, cnt, cl, epoch, budget, blocks, s);
+    case KIND_ALCUBIERRE: return launch_serve_fp64_k<KIND_ALCUBIERRE>(jobs, cnt, cl, epoch, budget, blocks, s);
+    case KIND_MORRIS_THORNE: return launch_serve_fp64_k<KIND_MORRIS_THORNE>(jobs, cnt, cl, epoch, budget, blocks, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Before each serving launch: advance the epoch, empty the output resume buffer
+// of every class and reset the resume claim counters.
+__global__ void serve_prologue_kernel(ServeClass* cls, int nclasses, unsigned* epoch) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const unsigned e = *epoch + 1u;
+  const int pout = (int)(e & 1u) ^ 1;
+  for (int c = 0; c < nclasses; ++c) {
+    cls[c].resume_count[pout] = 0;
+    cls[c].resume_claim = 0;
+  }
+  *epoch = e;
+}
+
+cudaError_t launch_serve_prologue(ServeClass* cls, int nclasses, unsigned* epoch, cudaStream_t s) {
+  serve_prologue_kernel<<<1, 32, 0, s>>>(cls, nclasses, epoch);
+  return cudaGetLastError();
 }
 
 template <int K, int SRC, int SINK>

@@ -17,6 +17,7 @@
 
 #include "internal.h"
 #include "metric_analytic.cuh"
+#include "serve_common.cuh"
 #include "trace_common.cuh"
 
 namespace geon {
@@ -60,7 +61,7 @@ struct MixedStepper {
   AConsts<double> Cd;
   float cap_hi, cap_lo, esc_hi, esc_lo;
   float h, hh, sixth;
-  unsigned since_renorm = 0;
+  unsigned nsteps = 0;  // steps this ray has taken: renormalisation follows the ray, not the lane
   bool ready = false;
 
   __device__ __forceinline__ void setup(const TraceLaunch& L) {
@@ -76,13 +77,18 @@ struct MixedStepper {
     ready = true;
   }
 
-  __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) {
-    if (!ready) setup(L);
+  __device__ __forceinline__ void load_state(const double y[8]) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      hi[i] = __double2float_rn(y0[i]);
-      lo[i] = __double2float_rn(y0[i] - (double)hi[i]);
+      hi[i] = __double2float_rn(y[i]);
+      lo[i] = __double2float_rn(y[i] - (double)hi[i]);
     }
+  }
+
+  __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) {
+    if (!ready) setup(L);
+    nsteps = 0;
+    load_state(y0);
   }
 
   __device__ __forceinline__ void to_double(double out[8]) const {
@@ -161,7 +167,7 @@ struct MixedStepper {
     }
 #pragma unroll
     for (int i = 4; i < 8; ++i) two_sum_update(hi[i], lo[i], inc[i]);
-    if ((++since_renorm & 7) == 0) {
+    if ((++nsteps & 7) == 0) {
 #pragma unroll
       for (int i = 0; i < 8; ++i) renormalise(hi[i], lo[i]);
     }
@@ -217,7 +223,8 @@ struct MixedStepper {
       finite &= isfinite(yn[i]);
     }
     if (!finite) return STEP_NONFINITE;
-    load(L, yn);
+    load_state(yn);
+    ++nsteps;
     return STEP_OK;
   }
 
@@ -228,6 +235,25 @@ struct MixedStepper {
   }
 
   __device__ __forceinline__ void finish(const TraceLaunch&) {}
+  // Serving: rays of different jobs pass through one lane, so the per-job
+  // constants are rebuilt when a lane takes a ray of another job.
+  __device__ __forceinline__ void rebind(const TraceLaunch& L) { setup(L); }
+  __device__ __forceinline__ void save(uint32_t w[16]) const {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      w[i] = __float_as_uint(hi[i]);
+      w[8 + i] = __float_as_uint(lo[i]);
+    }
+  }
+  __device__ __forceinline__ void restore(const TraceLaunch& L, const uint32_t w[16], int64_t n) {
+    setup(L);
+    nsteps = (unsigned)n;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      hi[i] = __uint_as_float(w[i]);
+      lo[i] = __uint_as_float(w[8 + i]);
+    }
+  }
 };
 
 // MINB is the register cap chosen by the autotuner: __launch_bounds__(128, MINB)
@@ -266,6 +292,37 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
     case 2: return launch_mst_v<K, SRC, SINK, 6>(L, s);
     default: return launch_mst_v<K, SRC, SINK, 1>(L, s);
   }
+}
+
+// Serving engine kernel for the mixed-precision classes (serve_common.cuh),
+// register cap of the autotuner's variant 1 (5 blocks per SM).
+template <int K>
+__global__ void __launch_bounds__(TRACE_BLOCK, 5) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
+                                                                     ServeClass* cl, const unsigned* epoch, int budget) {
+  serve_loop<MixedStepper<K>, K>(jobs, cnt, cl, epoch, budget);
+}
+
+int serve_mixed_blocks_per_sm(int kind) {
+  int occ = 0;
+  switch (kind) {
+    case KIND_MINKOWSKI: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_mixed_kernel<KIND_MINKOWSKI>, TRACE_BLOCK, 0); break;
+    case KIND_SCHWARZSCHILD: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_mixed_kernel<KIND_SCHWARZSCHILD>, TRACE_BLOCK, 0); break;
+    case KIND_ALCUBIERRE: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_mixed_kernel<KIND_ALCUBIERRE>, TRACE_BLOCK, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_mixed_kernel<KIND_MORRIS_THORNE>, TRACE_BLOCK, 0); break;
+  }
+  return occ < 1 ? 1 : occ;
+}
+
+cudaError_t launch_serve_mixed(int kind, const ServeJob* jobs, ServeCounters cnt, ServeClass* cl,
+                               const unsigned* epoch, int budget, int blocks, cudaStream_t s) {
+  switch (kind) {
+    case KIND_MINKOWSKI: serve_mixed_kernel<KIND_MINKOWSKI><<<blocks, TRACE_BLOCK, 0, s>>>(jobs, cnt, cl, epoch, budget); break;
+    case KIND_SCHWARZSCHILD: serve_mixed_kernel<KIND_SCHWARZSCHILD><<<blocks, TRACE_BLOCK, 0, s>>>(jobs, cnt, cl, epoch, budget); break;
+    case KIND_ALCUBIERRE: serve_mixed_kernel<KIND_ALCUBIERRE><<<blocks, TRACE_BLOCK, 0, s>>>(jobs, cnt, cl, epoch, budget); break;
+    case KIND_MORRIS_THORNE: serve_mixed_kernel<KIND_MORRIS_THORNE><<<blocks, TRACE_BLOCK, 0, s>>>(jobs, cnt, cl, epoch, budget); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 template <int K>

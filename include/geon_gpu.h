@@ -260,6 +260,79 @@ int geon_shadow_bisect_dev_noalloc(geon_metric_t schwarzschild, double r_obs, co
                                    int64_t max_steps, int precision, double* alpha_c,
                                    double* lo_out, double* hi_out, int64_t* steps_out, void* stream);
 
+/* --- serving engine (no counterpart in the reference) ---------------------------
+ * The reference renders one image per process (bin/render.rs:69-143), bisects in
+ * one loop (bin/validate_shadow.rs:70-77) and evaluates curvature point by point
+ * (curvature.rs:16-141). A server runs all three kinds of request for many
+ * callers at once on one GPU: requests are admitted while their buffers fit in a
+ * device memory budget fixed at creation, rays of every admitted request share
+ * persistent kernels that refill finished lanes from a device work queue, and
+ * a request that arrives while others run joins at the next kernel launch.
+ * Each result is the one the matching single-call entry point gives
+ * (geon_render_ex, geon_shadow_bisect with one bracket, geon_curvature_grid),
+ * bit for bit, whatever else runs beside it. */
+typedef struct geon_server* geon_server_t;
+enum geon_job_type { GEON_JOB_RENDER = 0, GEON_JOB_BISECT = 1, GEON_JOB_CURVATURE = 2 };
+
+typedef struct {
+  int32_t type;             /* geon_job_type */
+  int32_t metric_kind;      /* geon_metric_kind */
+  double metric_params[4];  /* as geon_metric_create */
+  int32_t nparams;
+  int32_t precision;        /* GEON_FP64 or GEON_MIXED (ray requests) */
+  double deadline_s;        /* > 0: give up after this many seconds (GEON_ERR_TIMEOUT) */
+  /* GEON_JOB_RENDER: geon_render_ex's arguments (render.precision is ignored) */
+  geon_camera camera;
+  geon_render_config render;
+  float* rgb;                     /* out: width*height*3 */
+  geon_render_stats* render_stats;/* out, may be NULL */
+  int32_t* pixel_class;           /* out, may be NULL */
+  int64_t* pixel_steps;           /* out, may be NULL */
+  /* GEON_JOB_BISECT: one bracket of geon_shadow_bisect (Schwarzschild only) */
+  double r_obs, lo, hi, step;
+  int64_t max_steps;
+  int32_t iters;            /* halvings */
+  int32_t rays_per_round;   /* 2^L - 1 speculative midpoints per round (L = 1..12; default 31) */
+  double* alpha_c;          /* out */
+  double* lo_out;           /* out, may be NULL */
+  double* hi_out;           /* out, may be NULL */
+  int64_t* steps_out;       /* out, may be NULL: steps of the rays on the bisection path */
+  /* GEON_JOB_CURVATURE: geon_curvature_grid's arguments */
+  geon_grid grid;
+  int64_t nk;
+  uint64_t seed;
+  double* einstein;         /* out, may be NULL */
+  double* nec;              /* out, may be NULL */
+} geon_job;
+
+typedef struct {
+  int64_t submitted, completed, failed, queued, running;
+  int64_t completed_by_type[3];
+  double p50_ms, p99_ms, mean_ms;           /* submission to completion, every type */
+  double p50_ms_by_type[3], p99_ms_by_type[3];
+  double ray_steps;                         /* ray-steps integrated for completed requests */
+  double grid_points;                       /* curvature points of completed requests */
+  double wall_s;                            /* first submission to last completion */
+  int64_t epochs;                           /* persistent-kernel launches */
+} geon_server_stats;
+
+/* budget_bytes: device memory for request buffers (a request larger than it is
+ * refused with GEON_ERR_ADMISSION at submission). */
+int geon_server_create(size_t budget_bytes, geon_server_t* out);
+/* Queue a request; output pointers must stay valid until it completes. */
+int geon_server_submit(geon_server_t s, const geon_job* job, uint64_t* id);
+/* 0 queued, 1 running, 2 done; a negative status if it failed. */
+int geon_server_poll(geon_server_t s, uint64_t id);
+/* Block until the request is done (timeout_s < 0: no limit); returns its status. */
+int geon_server_wait(geon_server_t s, uint64_t id, double timeout_s);
+int geon_server_wait_all(geon_server_t s, double timeout_s);
+/* A queued request is dropped; a running one stops at the next launch
+ * boundary. Its status becomes GEON_ERR_CANCELLED. */
+int geon_server_cancel(geon_server_t s, uint64_t id);
+int geon_server_stats_get(geon_server_t s, geon_server_stats* out);
+/* Stops the server after the work in flight; queued requests are cancelled. */
+int geon_server_destroy(geon_server_t s);
+
 /* --- measurement helpers (no counterpart in the reference) --------------------- */
 /* Kernels this library has launched since it was loaded. */
 unsigned long long geon_launch_count(void);

@@ -66,3 +66,43 @@ def test_show_stars_flag(lib):
     assert lib.geon_get_show_stars() == 0
     lib.geon_set_show_stars(1)
     assert lib.geon_get_show_stars() == 1
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes struct of the binding has the C header's size and field offsets."""
+    import shutil
+    import subprocess
+    from geon_gb300 import _ffi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"geon_camera": _ffi.GeonCamera, "geon_render_config": _ffi.GeonRenderConfig,
+               "geon_render_stats": _ffi.GeonRenderStats, "geon_grid": _ffi.GeonGrid,
+               "geon_job": _ffi.GeonJob, "geon_server_stats": _ffi.GeonServerStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "geon_gpu.h"', "int main(void) {"]
+    expect = []
+    for cname, cls in structs.items():
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        expect.append(ctypes.sizeof(cls))
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {fname}));')
+            expect.append(getattr(cls, fname).offset)
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == expect
+
+
+def test_server_argument_errors_without_gpu(lib):
+    from geon_gb300 import _ffi
+    h = ctypes.c_void_p()
+    assert lib.geon_server_create(16, ctypes.byref(h)) == -1
+    assert lib.geon_server_create(1 << 20, None) == -1
+    job = _ffi.GeonJob()
+    jid = ctypes.c_uint64()
+    assert lib.geon_server_submit(None, ctypes.byref(job), ctypes.byref(jid)) == -1
+    assert lib.geon_server_poll(None, 1) == -1
+    assert lib.geon_server_destroy(None) == 0
