@@ -12,8 +12,12 @@ would be 9.63 deg, outside them). Inputs are synthetic and seeded.
 
 value = useful ray-steps (sweep steps + the bisections' sequential-path steps)
 per second of device time with inputs resident in HBM. The default precision
-is the mixed FP32/FP64 path; the plain FP64 path is measured beside it on a
-uniform 1/32 sample of the sweep, and accuracy of mixed vs FP64 is reported.
+is the mixed FP32/FP64 path; the plain FP64 path is timed beside it on the
+same workload (one device-timed step), and the accuracy of mixed vs FP64 is
+reported on a uniform 1/32 sample of the sweep.
+`--workload serve` runs the serving stream instead (serve_requests): a seeded
+Poisson stream of render, bisection and curvature requests through
+geon_gb300.Server, mixed then FP64, with p50/p99 latency.
 `--impl reference` times the CPU restatement of the reference (oracle/) on
 the host cores instead.
 """
@@ -153,7 +157,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-rays", type=int, default=4096)
-    ap.add_argument("--fp64-sample", type=int, default=32, help="FP64 leg traces every k-th sweep ray")
+    ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy leg traces every k-th sweep ray")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 leg, accuracy, e2e and CPU legs")
     # small cases for profiling only (they change the workload; never a bench line)
     ap.add_argument("--rays", type=int, default=N_SWEEP, help="profiling: sweep size")
@@ -264,6 +268,20 @@ def main():
     sweep_steps = int(d_steps.sum().item())
     sweep_term = d_term.cpu().numpy()
     ac_mixed = d_ac.cpu().numpy()
+    fp64_leg = None
+    full = n_sweep == N_SWEEP and not args.sweep_only and args.escape_radius == SCHW[2]
+    if prec == 1 and full and not args.no_extras:
+        # the plain FP64 path on the same workload, one device-timed step
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev = one_step(0)
+        torch.cuda.synchronize()
+        ms64 = ev[0].elapsed_time(ev[1])
+        steps64 = int(d_steps.sum().item()) + int(d_bst.sum().item())
+        fp64_leg = {"value": steps64 / (ms64 / 1e3), "unit": "ray-steps/s", "ms_per_step": ms64,
+                    "sweep_ms": ev[2].elapsed_time(ev[3]), "bisection_ms": ev[4].elapsed_time(ev[5]),
+                    "sample": "the full workload, one step, CUDA events",
+                    "mixed_over_fp64": value / (steps64 / (ms64 / 1e3))}
 
     if rank != 0:
         if dist is not None:
@@ -285,8 +303,10 @@ def main():
                 "peak_source": "measured in this run: FFMA/DFMA throughput probe (geon_probe_fma_peak); "
                                "MEASURED_PEAKS.json has no FP32/FP64 non-tensor peak"}
 
-    if not args.no_extras and n_sweep == N_SWEEP and not args.sweep_only and args.escape_radius == SCHW[2]:
+    if not args.no_extras and full:
         extras = extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_mixed, prec, dev, value)
+    if fp64_leg is not None:
+        extras["fp64_path"] = fp64_leg
 
     line = {
         "metric": "ray-steps/s", "value": value, "unit": "ray-steps/s", "n_gpus": world, "steps": args.steps,
@@ -298,7 +318,8 @@ def main():
                                "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
                    "precision": args.precision, "rays_per_gpu": N_SWEEP, "bisections_per_gpu": N_BRACKETS,
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards",
-                   "mixed_kernel_variant": None if tuned is None else tuned["variant"][1]},
+                   "mixed_kernel_variant": None if tuned is None else tuned["variant"][1],
+                   "autotune_rates": None if tuned is None else tuned.get("rates")},
         "latency": {"bisection_ms_p50": float(np.percentile(bis_ms, 50)),
                     "bisection_ms_p99": float(np.percentile(bis_ms, 99)),
                     "sweep_ms_p50": float(np.percentile(sweep_ms, 50)),
@@ -332,17 +353,9 @@ def load_traffic():
 def extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_run, prec, dev, value):
     import torch
     out = {}
-    # FP64 path on a uniform sample of the sweep, and the FP64 bisections.
+    # Accuracy of the mixed path against the FP64 path on a uniform sample (full traces).
     k = args.fp64_sample
     sample = alpha[::k]
-    t0 = time.perf_counter()
-    t64, s64 = geon.shadow.classify(m, R_OBS, sample, STEP, MAX_STEPS, precision="fp64")
-    dt64 = time.perf_counter() - t0
-    fp64_rate = float(s64.sum()) / dt64
-    out["fp64_path"] = {"value": fp64_rate, "unit": "ray-steps/s",
-                        "sample": f"every {k}th sweep ray ({len(sample)} rays), host API wall time",
-                        "mixed_over_fp64": value / fp64_rate}
-    # Accuracy of the mixed path against the FP64 path on the same sample (full traces).
     y0 = geon.shadow.equatorial_ray(m, R_OBS, sample)
     r64 = geon.trace(m, y0, STEP, MAX_STEPS, precision="fp64")
     rmx = geon.trace(m, y0, STEP, MAX_STEPS, precision="mixed")
@@ -412,5 +425,134 @@ def extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_run, prec, dev,
     return out
 
 
+SERVE_RES = (128, 256, 512, 1024, 2048)
+
+
+def serve_requests(n, rate, seed):
+    """A seeded request stream: Poisson arrivals (mean `rate`/s); 60% renders
+    (metric uniform over the four, square resolution uniform over SERVE_RES,
+    camera at radius U[10, 40] looking at the origin, fov U[40, 90] deg),
+    30% shadow bisections (one bracket, 32 halvings, 31 rays per round),
+    10% curvature slabs of 32^3 points (16 null vectors per point)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for i in range(n):
+        u = rng.random()
+        if u < 0.6:
+            kind = int(rng.integers(0, 4))
+            res = int(SERVE_RES[rng.integers(0, len(SERVE_RES))])
+            r = float(rng.uniform(10.0, 40.0))
+            fov = float(rng.uniform(40.0, 90.0))
+            reqs.append(("render", float(t[i]), kind, res, r, fov))
+        elif u < 0.9:
+            reqs.append(("bisect", float(t[i]), float(np.radians(rng.uniform(13.0, 14.0))),
+                         float(np.radians(rng.uniform(14.5, 15.5)))))
+        else:
+            reqs.append(("curvature", float(t[i]), int(rng.integers(0, 4)), int(rng.integers(0, 1 << 62))))
+    return reqs
+
+
+def run_serve_stream(geon, reqs, precision, budget):
+    """Submit the stream at its arrival times; returns the server's statistics."""
+    metrics = {0: geon.Minkowski(), 1: geon.Schwarzschild(1.0, 1.001, 100.0),
+               2: geon.Alcubierre(2.0, 0.125, 0.5, 0.0), 3: geon.MorrisThorne(1.0)}
+    sch = geon.Schwarzschild(1.0)
+    grids = {0: ((-10.0, -10.0, -10.0), (10.0, 10.0, 10.0)), 1: ((3.0, 0.3, 0.0), (10.0, 2.8, 6.0)),
+             2: ((-4.0, -4.0, -4.0), (4.0, 4.0, 4.0)), 3: ((-5.0, 0.3, 0.0), (5.0, 2.8, 6.0))}
+    jobs = []
+    with geon.Server(budget) as srv:
+        t0 = time.perf_counter()
+        for q in reqs:
+            wait = q[1] - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            if q[0] == "render":
+                _, _, kind, res, r, fov = q
+                if kind in (1, 3):
+                    obs, fwd = [0.0, r, np.pi / 2, 0.0], 1
+                elif kind == 2:
+                    obs, fwd = [0.0, -r, 0.0, 0.0], -1
+                else:
+                    obs, fwd = [0.0, r, 0.0, 0.0], 1
+                cam = geon.Camera(obs, fov, res, res, forward_sign=fwd)
+                jobs.append(srv.submit_render(metrics[kind], cam, geon.RenderConfig(show_stars=True),
+                                              precision=precision))
+            elif q[0] == "bisect":
+                jobs.append(srv.submit_bisect(sch, R_OBS, q[2], q[3], iters=32, precision=precision,
+                                              rays_per_round=31))
+            else:
+                lo, hi = grids[q[2]]
+                jobs.append(srv.submit_curvature(metrics[q[2]], lo, hi, (32, 32, 32), nk=16, seed=q[3],
+                                                 with_einstein=True))
+        t_submitted = time.perf_counter() - t0
+        srv.wait_all()
+        t_all = time.perf_counter() - t0
+        st = srv.stats()
+        failed = [j.id for j in jobs if j.poll() != 2]
+    st["submit_wall_s"] = t_submitted
+    st["drain_wall_s"] = t_all
+    st["failed_ids"] = failed[:10]
+    return st
+
+
+def serve_main(args):
+    """The serving stream, mixed then FP64, as one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    import geon_gb300 as geon
+    lib = geon._load()
+    for kind_metric in (geon.Schwarzschild(1.0, 1.001, 100.0), geon.Alcubierre(2.0, 0.125, 0.5, 0.0),
+                        geon.MorrisThorne(1.0), geon.Minkowski()):
+        geon.autotune.autotune(kind_metric)
+    reqs = serve_requests(args.requests, args.rate, 0x5E4E)
+    sampler = ClockSampler(0)
+    sampler.start()
+    launches0 = lib.geon_launch_count()
+    legs = {}
+    for prec in args.serve_precisions.split(","):
+        legs[prec] = run_serve_stream(geon, reqs, prec, args.budget_gb << 30)
+    launches = lib.geon_launch_count() - launches0
+    clocks = sampler.stop()
+    n_types = {k: sum(1 for q in reqs if q[0] == k) for k in ("render", "bisect", "curvature")}
+    offered_s = reqs[-1][1]
+    out = {}
+    for prec, st in legs.items():
+        out[prec] = {"ray_steps_per_s": st["ray_steps"] / st["drain_wall_s"],
+                     "grid_points_per_s": st["grid_points"] / st["drain_wall_s"],
+                     "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "by_type": st["by_type"],
+                     "completed": st["completed"], "failed": st["failed"],
+                     "offered_requests_per_s": len(reqs) / offered_s,
+                     "sustained_requests_per_s": st["completed"] / st["drain_wall_s"],
+                     "drain_wall_s": st["drain_wall_s"], "launches": st["launches"]}
+    main_prec = args.serve_precisions.split(",")[0]
+    line = {"metric": "ray-steps/s", "value": out[main_prec]["ray_steps_per_s"], "unit": "ray-steps/s",
+            "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * legs[main_prec]["drain_wall_s"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 with f64 band (mixed)" if main_prec == "mixed" else "f64",
+            "data": "synthetic seeded request stream",
+            "config": {"workload": f"serving stream: {len(reqs)} requests, Poisson mean {args.rate}/s "
+                                   f"({n_types['render']} renders 128^2-2048^2 over 4 metrics, "
+                                   f"{n_types['bisect']} 32-halving bisections, {n_types['curvature']} "
+                                   f"32^3 curvature slabs)", "budget_gb": args.budget_gb,
+                       "timing": "host wall clock, first submission to last completion"},
+            "serving": out, "gpu_launches": int(launches), "clocks": clocks}
+    if "mixed" in out and "fp64" in out:
+        line["serving"]["mixed_over_fp64_ray_steps"] = out["mixed"]["ray_steps_per_s"] / out["fp64"]["ray_steps_per_s"]
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
-    main()
+    if "--workload" in sys.argv and "serve" in sys.argv:
+        ap = argparse.ArgumentParser()
+        ap.add_argument("--workload", choices=["serve"])
+        ap.add_argument("--requests", type=int, default=200)
+        ap.add_argument("--rate", type=float, default=200.0)
+        ap.add_argument("--budget-gb", type=int, default=64)
+        ap.add_argument("--serve-precisions", default="mixed,fp64")
+        ap.add_argument("--gpus", type=int, default=1)
+        ap.add_argument("--steps", type=int, default=1)
+        ap.add_argument("--warmup", type=int, default=3)
+        serve_main(ap.parse_args())
+    else:
+        main()

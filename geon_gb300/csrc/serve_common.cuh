@@ -98,7 +98,13 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
       }
       need = __ballot_sync(FULL, slot < 0);
     }
-    unsigned pos = jobs_open ? atomicAdd(&cl->head, 0u) : tail;
+    // one read of the shared head per warp: every lane must walk the same ring
+    // positions, since lane offsets are taken from the leader's claim
+    unsigned pos = tail;
+    if (jobs_open) {
+      if (lane == 0) pos = atomicAdd(&cl->head, 0u);
+      pos = __shfl_sync(FULL, pos, 0);
+    }
     while (need && jobs_open) {
       if (pos >= tail) {
         jobs_open = false;

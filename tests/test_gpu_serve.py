@@ -163,3 +163,29 @@ def test_latency_stats(geon):
     assert st["by_type"]["curvature"]["completed"] == 1 and st["grid_points"] == 64
     assert 0 < st["p50_ms"] <= st["p99_ms"]
     assert st["ray_steps"] == total
+
+
+def test_many_jobs_per_class(geon):
+    """Twenty renders of different sizes in the same two classes, in flight at
+    once with bisections: every ray is claimed exactly once."""
+    sch = geon.Schwarzschild(1.0, 1.001, 100.0)
+    rng = np.random.default_rng(5)
+    cases = []
+    with geon.Server(1 << 30) as srv:
+        jobs = []
+        for i in range(20):
+            w, h = int(rng.integers(8, 48)), int(rng.integers(8, 48))
+            r = float(rng.uniform(12.0, 40.0))
+            cam = geon.Camera([0.0, r, np.pi / 2, 0.0], float(rng.uniform(40.0, 90.0)), w, h)
+            cfg = geon.RenderConfig(precision="mixed" if i % 2 else "fp64", show_stars=True)
+            jobs.append(srv.submit_render(sch, cam, cfg))
+            cases.append((cam, cfg))
+        bis = [srv.submit_bisect(geon.Schwarzschild(1.0), R_OBS, np.radians(13.0), np.radians(15.5), iters=20,
+                                 precision=p) for p in ("fp64", "mixed", "fp64", "mixed")]
+        srv.wait_all(timeout=300)
+        for j, (cam, cfg) in zip(jobs, cases):
+            same_render(single_render(geon, sch, cam, cfg), j.result())
+        for j, p in zip(bis, ("fp64", "mixed", "fp64", "mixed")):
+            ac, lo, hi, st = geon.shadow.bisect(geon.Schwarzschild(1.0), R_OBS, np.radians(13.0),
+                                                np.radians(15.5), iters=20, precision=p)
+            assert j.result()["alpha_c"] == ac[0] and j.result()["steps"] == st[0]
