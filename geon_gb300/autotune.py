@@ -34,13 +34,13 @@ def _load():
         return {}
 
 
-def autotune(metric, n_rays=65536, max_steps=20000, use_cache=True):
+def autotune(metric, n_rays=0, max_steps=20000, use_cache=True):
     """Pick the fastest variant per ray source for metric's kind.
 
     Returns {"variant": [camera/array source, equatorial source], "rates": ...}.
     """
     lib = _ffi.load()
-    key = f"{_gpu_name()}|kind={metric.kind}"
+    key = f"{_gpu_name()}|kind={metric.kind}|rays={n_rays}|steps={max_steps}"
     cache = _load() if use_cache else {}
     if key in cache:
         for src, v in enumerate(cache[key]["variant"]):

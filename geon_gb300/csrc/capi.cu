@@ -291,7 +291,15 @@ static int time_variants(const TraceLaunch& base, int src, int sink, int64_t n, 
 
 int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, double* rates_out, int* best_out) {
   if (int rc = check_metric(m)) return rc;
-  if (n_rays <= 0 || max_steps <= 0) return fail(GEON_ERR_INVALID, "bad calibration size");
+  if (n_rays < 0 || max_steps <= 0) return fail(GEON_ERR_INVALID, "bad calibration size");
+  if (n_rays == 0) {
+    // four rays per lane of the largest variant's grid: occupancy decides the
+    // rate only when every lane has work for most of the launch
+    int dev = 0, sms = 0;
+    GEON_CUDA(cudaGetDevice(&dev));
+    GEON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    n_rays = (int64_t)sms * 6 * 128 * 4;  // 128 threads per trace block
+  }
   const int kind = m->desc.kind;
   double rates[6] = {0, 0, 0, 0, 0, 0};
   int best[2] = {0, -1};

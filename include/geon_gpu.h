@@ -174,8 +174,8 @@ void geon_set_persistent_reserve(int blocks_per_sm);
 /* Register-cap variant of the mixed kernel per metric kind and ray source
  * (source 0: camera rays and ray arrays, 1: equatorial shadow rays): 0 = no
  * cap, 1 = fit 5 blocks of 128 threads per SM, 2 = fit 6. geon_autotune_mixed
- * times every variant on calibration jobs of this metric (n_rays rays, at most
- * max_steps each; the equatorial job only for Schwarzschild), selects the
+ * times every variant on calibration jobs of this metric (n_rays rays - 0 picks
+ * four per lane of the widest grid - at most max_steps each; the equatorial job only for Schwarzschild), selects the
  * fastest per source and writes ray-steps/s per (source, variant) to
  * rates_out[6] and the choices to best_out[2] (-1 = source not tuned); either
  * may be NULL. */
