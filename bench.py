@@ -512,6 +512,7 @@ def serve_main(args):
     legs = {}
     for prec in args.serve_precisions.split(","):
         legs[prec] = run_serve_stream(geon, reqs, prec, args.budget_gb << 30)
+        print(f"serving leg {prec}: " + json.dumps(legs[prec]), file=sys.stderr, flush=True)
     launches = lib.geon_launch_count() - launches0
     clocks = sampler.stop()
     n_types = {k: sum(1 for q in reqs if q[0] == k) for k in ("render", "bisect", "curvature")}
