@@ -12,8 +12,8 @@ would be 9.63 deg, outside them). Inputs are synthetic and seeded.
 
 value = useful ray-steps (sweep steps + the bisections' sequential-path steps)
 per second of device time with inputs resident in HBM. The default precision
-is the mixed FP32/FP64 path; the plain FP64 path is timed beside it on the
-same workload (one device-timed step), and the accuracy of mixed vs FP64 is
+is the mixed FP32/FP64 path; the plain FP64 path is timed beside it (one
+device-timed step over every 4th sweep ray and the bisections), and the accuracy of mixed vs FP64 is
 reported on a uniform 1/32 sample of the sweep.
 `--workload serve` runs the serving stream instead (serve_requests): a seeded
 Poisson stream of render, bisection and curvature requests through
@@ -204,7 +204,8 @@ def main():
         if rc != 0:
             raise RuntimeError(lib.geon_last_error().decode())
 
-    def one_step(precision):
+    def one_step(precision, sweep=None):
+        s_alpha, s_n = sweep if sweep is not None else (d_alpha, n_sweep)
         main = torch.cuda.current_stream()
         e0 = torch.cuda.Event(enable_timing=True)
         ea0, ea1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -215,7 +216,7 @@ def main():
         sb.wait_stream(main)
         ea0.record(sa)
         lib.geon_set_persistent_reserve(RESERVE)  # leave room on every SM for the bisection rounds
-        check(lib.geon_shadow_classify_dev(h, R_OBS, d_alpha.data_ptr(), n_sweep, STEP, MAX_STEPS, precision,
+        check(lib.geon_shadow_classify_dev(h, R_OBS, s_alpha.data_ptr(), s_n, STEP, MAX_STEPS, precision,
                                            d_term.data_ptr(), d_steps.data_ptr(), sa.cuda_stream))
         lib.geon_set_persistent_reserve(0)
         ea1.record(sa)
@@ -271,16 +272,20 @@ def main():
     fp64_leg = None
     full = n_sweep == N_SWEEP and not args.sweep_only and args.escape_radius == SCHW[2]
     if prec == 1 and full and not args.no_extras:
-        # the plain FP64 path on the same workload, one device-timed step
+        # The plain FP64 path, device-timed on the same kind of step: every 4th
+        # sweep ray (262144 rays, over 3 rays per resident FP64 lane) plus all
+        # 64 bisections. (GB300 runs FP64 at 1/62 of its FP32 rate; the full
+        # sweep would take minutes.)
+        sub = d_alpha[::4].contiguous()
         flush.zero_()
         torch.cuda.synchronize()
-        ev = one_step(0)
+        ev = one_step(0, (sub, sub.numel()))
         torch.cuda.synchronize()
         ms64 = ev[0].elapsed_time(ev[1])
-        steps64 = int(d_steps.sum().item()) + int(d_bst.sum().item())
+        steps64 = int(d_steps[:sub.numel()].sum().item()) + int(d_bst.sum().item())
         fp64_leg = {"value": steps64 / (ms64 / 1e3), "unit": "ray-steps/s", "ms_per_step": ms64,
                     "sweep_ms": ev[2].elapsed_time(ev[3]), "bisection_ms": ev[4].elapsed_time(ev[5]),
-                    "sample": "the full workload, one step, CUDA events",
+                    "sample": "every 4th sweep ray + the 64 bisections, one step, CUDA events",
                     "mixed_over_fp64": value / (steps64 / (ms64 / 1e3))}
 
     if rank != 0:
@@ -425,6 +430,214 @@ def extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_run, prec, dev,
     return out
 
 
+def _wall(fn, reps):
+    """Best-of-reps wall time of fn() (host API calls return with results on the host)."""
+    best, out = 1e30, None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = fn()
+        best = min(best, time.perf_counter() - t0)
+    return best, out
+
+
+def _emit(workload, value, unit, ms, dtype, extra):
+    line = {"metric": unit, "value": value, "unit": unit, "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": dtype, "data": "synthetic (seeded)", "config": {"workload": workload}}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def reference_gpu_bar(width, height, r_obs, fov_deg, step, max_steps, reps=5):
+    """The reference's own CUDA kernel (cuda/schwarzschild_render.cu trace_kernel,
+    compiled from its source by oracle/ref_cu.py) launched as its main() does:
+    16x16 blocks, one pixel per thread, M 1, horizon_pad 1.001, escape 1000M.
+    Returns its best-of-reps kernel wall time and termination counts."""
+    import ctypes
+    from oracle import ref_cu
+    if not os.path.exists(ref_cu.CUBIN):
+        return {"unavailable": "oracle/_ref cubin not built (needs the reference checkout at build time)"}
+    cu = ctypes.CDLL("libcuda.so.1")
+
+    def ok(rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what}: CUresult {rc}")
+
+    ctx = ctypes.c_void_p()
+    ok(cu.cuCtxGetCurrent(ctypes.byref(ctx)), "cuCtxGetCurrent")
+    if not ctx.value:
+        dev = ctypes.c_int()
+        ok(cu.cuDeviceGet(ctypes.byref(dev), 0), "cuDeviceGet")
+        ok(cu.cuDevicePrimaryCtxRetain(ctypes.byref(ctx), dev), "cuDevicePrimaryCtxRetain")
+        ok(cu.cuCtxSetCurrent(ctx), "cuCtxSetCurrent")
+    mod, fn = ctypes.c_void_p(), ctypes.c_void_p()
+    ok(cu.cuModuleLoad(ctypes.byref(mod), ref_cu.CUBIN.encode()), "cuModuleLoad")
+    ok(cu.cuModuleGetFunction(ctypes.byref(fn), mod, ref_cu.KERNEL.encode()), "cuModuleGetFunction")
+    n = width * height
+    d_term, d_final = ctypes.c_uint64(), ctypes.c_uint64()
+    ok(cu.cuMemAlloc_v2(ctypes.byref(d_term), ctypes.c_size_t(n * 4)), "cuMemAlloc")
+    ok(cu.cuMemAlloc_v2(ctypes.byref(d_final), ctypes.c_size_t(n * 64)), "cuMemAlloc")
+    vals = [ctypes.c_int(width), ctypes.c_int(height), ctypes.c_double(r_obs),
+            ctypes.c_double(fov_deg * 3.141592653589793 / 180.0), ctypes.c_double(1.0), ctypes.c_double(step),
+            ctypes.c_int(max_steps), ctypes.c_double(1.001), ctypes.c_double(1000.0), d_term, d_final]
+    params = (ctypes.c_void_p * len(vals))(*[ctypes.addressof(v) for v in vals])
+    gx, gy = (width + 15) // 16, (height + 15) // 16
+    best = 1e30
+    for _ in range(reps + 1):
+        t0 = time.perf_counter()
+        ok(cu.cuLaunchKernel(fn, gx, gy, 1, 16, 16, 1, 0, None, params, None), "cuLaunchKernel")
+        ok(cu.cuCtxSynchronize(), "cuCtxSynchronize")
+        best = min(best, time.perf_counter() - t0)
+    term = np.empty(n, dtype=np.int32)
+    ok(cu.cuMemcpyDtoH_v2(term.ctypes.data_as(ctypes.c_void_p), d_term, ctypes.c_size_t(n * 4)), "cuMemcpyDtoH")
+    cu.cuMemFree_v2(d_term)
+    cu.cuMemFree_v2(d_final)
+    cu.cuModuleUnload(mod)
+    return {"ms": 1e3 * best, "rays_per_s": n / best, "captured": int(np.sum(term == 1)),
+            "escaped": int(np.sum(term == 2)), "diverged": int(np.sum(term == 0)),
+            "launch": f"{gx}x{gy} blocks of 16x16, best of {reps} after one warm-up, wall time around launch+sync"}
+
+
+def render_main(args):
+    """Schwarzschild 256^2 render (r 30M, fov 60, h 0.05, cap 20000, escape 100M, stars on):
+    FP64 and mixed through the host API, the oracle on every host core, and the
+    FP64 path at the reference CUDA program's own settings (escape 1000M)."""
+    import geon_gb300 as geon
+    from oracle import oracle as orc
+    geon._load()
+    obs = [0.0, 30.0, np.pi / 2, 0.0]
+    cam = geon.Camera(obs, 60.0, 256, 256)
+    m = geon.Schwarzschild(1.0, 1.001, 100.0)
+    geon.autotune.autotune(m)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        cfg = geon.RenderConfig(precision=prec, show_stars=True)
+        geon.render(m, cam, cfg)
+        dt, (rgb, st, cls, pst) = _wall(lambda: geon.render(m, cam, cfg, with_classes=True), 5)
+        res[prec] = {"ray_steps_per_s": st.total_steps / dt, "ms": 1e3 * dt, "total_steps": st.total_steps,
+                     "captured": st.captured, "escaped": st.escaped, "diverged": st.diverged, "cls": cls}
+    m1000 = geon.Schwarzschild(1.0, 1.001, 1000.0)
+    cfg = geon.RenderConfig(precision="fp64", show_stars=True)
+    geon.render(m1000, cam, cfg)
+    dt1000, (_, st1000) = _wall(lambda: geon.render(m1000, cam, cfg), 5)
+    ref_bar = reference_gpu_bar(256, 256, 30.0, 60.0, 0.05, 20000)
+    threads = orc.hardware_threads()
+    t0 = time.perf_counter()
+    _, ocls, opst, ost = orc.render(1, [1.0, 1.001, 100.0], obs, 60.0, 256, 256, 0.05, 20000, math=orc.LIBM,
+                                    nthreads=threads)
+    dt_cpu = time.perf_counter() - t0
+    cpu_rate = ost["total_steps"] / dt_cpu if "total_steps" in ost else float(opst.sum()) / dt_cpu
+    mism = float(np.mean(res["mixed"]["cls"] != res["fp64"]["cls"]))
+    exact = bool(np.array_equal(res["fp64"]["cls"], ocls))
+    for r in res.values():
+        r.pop("cls")
+    _emit("schwarzschild render 256x256, r_obs 30M, fov 60, h 0.05, cap 20000, escape 100M, stars on",
+          res["mixed"]["ray_steps_per_s"], "ray-steps/s", res["mixed"]["ms"], "f32 (mixed)",
+          {"render": res, "pixel_class_mismatch_mixed_vs_fp64": mism,
+           "fp64_pixel_classes_equal_oracle_libm": exact,
+           "reference_cuda_kernel_escape_1000M": ref_bar,
+           "fp64_escape_1000M": {"ms": 1e3 * dt1000, "total_steps": st1000.total_steps,
+                                 "ray_steps_per_s": st1000.total_steps / dt1000,
+                                 "captured": st1000.captured, "escaped": st1000.escaped,
+                                 "diverged": st1000.diverged,
+                                 "note": "the reference CUDA program's settings: 256x256 r 30 fov 60 h 0.05 "
+                                         "cap 20000, escape fixed at 1000M"},
+           "cpu_baseline": {"value": cpu_rate, "unit": "ray-steps/s", "cores": threads, "kind": "port",
+                            "sample": f"the full 256x256 image ({dt_cpu:.1f} s)"},
+           "timing": "host API wall time, best of 5, inputs and outputs on the host"})
+
+
+def exotic_main(args):
+    """2048^2 Alcubierre (R 2, thickness 0.125, v 0.5, observer x = -10 looking +x)
+    and Morris-Thorne (b0 1, observer l = 10) renders, fov 90, h 0.05, cap 20000:
+    mixed on the full image; FP64 on every 16th row; the oracle on one row."""
+    import geon_gb300 as geon
+    from oracle import oracle as orc
+    geon._load()
+    cases = {"alcubierre": (geon.Alcubierre(2.0, 0.125, 0.5, 0.0), 2, [2.0, 0.125, 0.5, 0.0],
+                            [0.0, -10.0, 0.0, 0.0], -1),
+             "morris_thorne": (geon.MorrisThorne(1.0), 3, [1.0], [0.0, 10.0, np.pi / 2, 0.0], 1)}
+    n = args.size
+    out = {}
+    threads = orc.hardware_threads()
+    for name, (m, kind, params, obs, fwd) in cases.items():
+        geon.autotune.autotune(m)
+        cam = geon.Camera(obs, 90.0, n, n, forward_sign=fwd)
+        cfg = geon.RenderConfig(precision="mixed", show_stars=True)
+        geon.render(m, geon.Camera(obs, 90.0, 64, 64, forward_sign=fwd), cfg)
+        dt, (_, st) = _wall(lambda: geon.render(m, cam, cfg), 1)
+        tet = cam.tetrad(m)
+        rows = np.arange(0, n, 16)
+        y0 = cam.ray_states(tet).reshape(n, n, 8)[rows].reshape(-1, 8)
+        t0 = time.perf_counter()
+        r64 = geon.trace(m, y0, 0.05, 20000, precision="fp64")
+        dt64 = time.perf_counter() - t0
+        rmx = geon.trace(m, y0, 0.05, 20000, precision="mixed")
+        p64, pmx = r64.termination, rmx.termination
+        esc = (p64 == 2) & (pmx == 2)
+        d64 = m.asymptotic_direction(r64.final_state[esc])
+        dmx = m.asymptotic_direction(rmx.final_state[esc])
+        ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0)) if esc.any() else np.zeros(1)
+        yc = y0[: n]  # the first sampled row
+        t0 = time.perf_counter()
+        _, _, osteps, _ = orc.trace(kind, params, yc, 0.05, 20000, math=orc.LIBM, nthreads=threads)
+        dt_cpu = time.perf_counter() - t0
+        out[name] = {"mixed_ray_steps_per_s": st.total_steps / dt, "mixed_ms": 1e3 * dt,
+                     "mixed_total_steps": st.total_steps,
+                     "fp64_ray_steps_per_s": float(r64.steps_taken.sum()) / dt64,
+                     "fp64_sample": f"every 16th row ({len(y0)} rays), host API wall time",
+                     "mixed_over_fp64": (st.total_steps / dt) / (float(r64.steps_taken.sum()) / dt64),
+                     "class_mismatch_mixed_vs_fp64": float(np.mean(p64 != pmx)),
+                     "escape_dir_err_rad_p50": float(np.median(ang)), "escape_dir_err_rad_max": float(ang.max()),
+                     "cpu_baseline": {"value": float(osteps.sum()) / dt_cpu, "unit": "ray-steps/s", "cores": threads,
+                                      "kind": "port", "sample": f"row 0 ({len(yc)} rays, {dt_cpu:.1f} s)"}}
+    v = sum(o["mixed_total_steps"] for o in out.values()) / sum(o["mixed_ms"] / 1e3 for o in out.values())
+    _emit(f"exotic renders {n}x{n}: alcubierre (R 2, thickness 0.125, v 0.5) and morris-thorne (b0 1), fov 90, "
+          "h 0.05, cap 20000", v, "ray-steps/s", sum(o["mixed_ms"] for o in out.values()), "f32 (mixed)",
+          {"exotic": out, "timing": "host API wall time"})
+
+
+def curvature_main(args):
+    """Curvature grid jobs (FP64): 128^3 Alcubierre (v 2, R 2, thickness 0.5)
+    Einstein + T(k,k) for 16 null vectors per point; a 4096-point Morris-Thorne
+    line; 1e5 Schwarzschild vacuum points (Ricci scalar)."""
+    import geon_gb300 as geon
+    from oracle import oracle as orc
+    geon._load()
+    threads = orc.hardware_threads()
+    alc = geon.Alcubierre(2.0, 0.5, 2.0, 0.0)
+    n = args.grid
+    geon.curvature.grid(alc, (-4, -4, -4), (4, 4, 4), (8, 8, 8), nk=16)
+    dt, (pts, ein, nec, _) = _wall(lambda: geon.curvature.grid(alc, (-4, -4, -4), (4, 4, 4), (n, n, n), nk=16), 2)
+    sub = np.arange(0, len(pts), max(1, len(pts) // 2048))
+    t0 = time.perf_counter()
+    oein = orc.curvature(2, [2.0, 0.5, 2.0, 0.0], pts[sub], "einstein", math=orc.GEON, nthreads=threads)
+    dt_cpu = time.perf_counter() - t0
+    bit_exact = bool(np.array_equal(oein.reshape(-1, 16), ein[sub].reshape(-1, 16)))
+    oein_libm = orc.curvature(2, [2.0, 0.5, 2.0, 0.0], pts[sub], "einstein", math=orc.LIBM, nthreads=threads)
+    err_libm = float(np.max(np.abs(oein_libm.reshape(-1, 16) - ein[sub].reshape(-1, 16))))
+    mt = geon.MorrisThorne(1.0)
+    dt_mt, (mpts, mein, mnec, _) = _wall(lambda: geon.curvature.grid(mt, (-5, np.pi / 2, 0), (5, np.pi / 2, 0),
+                                                                     (4096, 1, 1), nk=16), 3)
+    rng = np.random.default_rng(7)
+    x = np.stack([np.zeros(100000), rng.uniform(3.0, 30.0, 100000), rng.uniform(0.3, 2.8, 100000),
+                  rng.uniform(0.0, 6.2, 100000)], axis=1)
+    sch = geon.Schwarzschild(1.0)
+    dt_s, rs = _wall(lambda: geon.curvature.ricci_scalar(sch, x), 3)
+    _emit(f"curvature grid {n}^3 alcubierre (v 2, R 2, thickness 0.5) einstein + 16 null T(k,k) per point",
+          len(pts) / dt, "grid-points/s", 1e3 * dt, "f64",
+          {"curvature": {"alcubierre_grid": {"points": len(pts), "ms": 1e3 * dt, "points_per_s": len(pts) / dt,
+                                             "bit_exact_vs_oracle_geon_sample": bit_exact,
+                                             "max_abs_diff_vs_oracle_libm": err_libm},
+                         "morris_thorne_line": {"points": 4096, "ms": 1e3 * dt_mt, "points_per_s": 4096 / dt_mt,
+                                                "T_tt_throat_check": "tests/test_gpu_curvature_grid.py"},
+                         "schwarzschild_vacuum": {"points": 100000, "ms": 1e3 * dt_s, "points_per_s": 1e5 / dt_s,
+                                                  "max_abs_ricci_scalar": float(np.max(np.abs(rs)))}},
+           "cpu_baseline": {"value": len(sub) / dt_cpu, "unit": "grid-points/s", "cores": threads, "kind": "port",
+                            "sample": f"{len(sub)} grid points, einstein only ({dt_cpu:.1f} s)"},
+           "timing": "host API wall time (includes the copy of results to the host)"})
+
+
 SERVE_RES = (128, 256, 512, 1024, 2048)
 
 
@@ -544,16 +757,19 @@ def serve_main(args):
 
 
 if __name__ == "__main__":
-    if "--workload" in sys.argv and "serve" in sys.argv:
+    if "--workload" in sys.argv:
         ap = argparse.ArgumentParser()
-        ap.add_argument("--workload", choices=["serve"])
+        ap.add_argument("--workload", choices=["serve", "render", "exotic", "curvature"])
         ap.add_argument("--requests", type=int, default=200)
         ap.add_argument("--rate", type=float, default=200.0)
         ap.add_argument("--budget-gb", type=int, default=64)
         ap.add_argument("--serve-precisions", default="mixed,fp64")
+        ap.add_argument("--size", type=int, default=2048, help="exotic: image side")
+        ap.add_argument("--grid", type=int, default=128, help="curvature: grid side")
         ap.add_argument("--gpus", type=int, default=1)
         ap.add_argument("--steps", type=int, default=1)
         ap.add_argument("--warmup", type=int, default=3)
-        serve_main(ap.parse_args())
+        a = ap.parse_args()
+        {"serve": serve_main, "render": render_main, "exotic": exotic_main, "curvature": curvature_main}[a.workload](a)
     else:
         main()
