@@ -209,14 +209,14 @@ struct geon_server {
   ServeClass* d_cls = nullptr;
   unsigned long long* d_counters = nullptr;  // next | done | steps, SERVE_MAX_JOBS each
   unsigned* d_cancel = nullptr;
-  unsigned long long* h_counters = nullptr;  // pinned copy of done | steps
+  unsigned long long* h_counters = nullptr;  // pinned copy of next | done | steps
   int* h_flags = nullptr;                    // pinned, one per slot (curvature singular flag)
   ServeJob* h_jobs = nullptr;                // pinned staging of descriptors
   int* d_rings = nullptr;
   ResumeEntry* d_resume = nullptr;
   unsigned* d_epoch = nullptr;
-  unsigned* h_tail = nullptr;                // pinned, one per class
-  int* h_ring_slot = nullptr;                // pinned staging of ring entries, one per slot
+  int* h_order = nullptr;                    // pinned claim order, SERVE_RING per class
+  unsigned* h_tail_head = nullptr;           // pinned (tail, head = 0) per class
   unsigned* h_one = nullptr;                 // pinned constant 1
   int blocks[SERVE_CLASSES] = {};
   int iters[SERVE_CLASSES] = {};
@@ -247,7 +247,16 @@ namespace {
 int build_graph(geon_server* S) {
   cudaGraph_t g = nullptr;
   if (cudaStreamBeginCapture(S->s_main, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GEON_ERR_CUDA;
-  cudaError_t e = launch_serve_prologue(S->d_cls, SERVE_CLASSES, S->d_epoch, S->s_main);
+  // the claim order the host wrote for this launch, and (tail, head = 0)
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < SERVE_CLASSES && e == cudaSuccess; ++c) {
+    e = cudaMemcpyAsync(S->d_rings + (size_t)c * SERVE_RING, S->h_order + (size_t)c * SERVE_RING,
+                        sizeof(int) * SERVE_RING, cudaMemcpyHostToDevice, S->s_main);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&S->d_cls[c].tail, S->h_tail_head + 2 * c, 2 * sizeof(unsigned), cudaMemcpyHostToDevice,
+                          S->s_main);
+  }
+  if (e == cudaSuccess) e = launch_serve_prologue(S->d_cls, SERVE_CLASSES, S->d_epoch, S->s_main);
   if (e == cudaSuccess) e = cudaEventRecord(S->ev_fork, S->s_main);
   ServeCounters cnt{S->d_counters, S->d_counters + SERVE_MAX_JOBS, S->d_counters + 2 * SERVE_MAX_JOBS,
                     S->d_cancel};
@@ -264,8 +273,8 @@ int build_graph(geon_server* S) {
     if (e == cudaSuccess) e = cudaStreamWaitEvent(S->s_main, S->ev_join[c], 0);
   }
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(S->h_counters, S->d_counters + SERVE_MAX_JOBS,
-                        sizeof(unsigned long long) * 2 * SERVE_MAX_JOBS, cudaMemcpyDeviceToHost, S->s_main);
+    e = cudaMemcpyAsync(S->h_counters, S->d_counters, sizeof(unsigned long long) * 3 * SERVE_MAX_JOBS,
+                        cudaMemcpyDeviceToHost, S->s_main);
   const cudaError_t e2 = cudaStreamEndCapture(S->s_main, &g);
   if (e != cudaSuccess || e2 != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
@@ -276,30 +285,39 @@ int build_graph(geon_server* S) {
   return e3 == cudaSuccess ? GEON_OK : GEON_ERR_CUDA;
 }
 
-// Publish a ray job: descriptor, zeroed counters, cancel flag cleared, ring
-// entry, class tail. Copies are stream-ordered before the next launch.
+// Publish a ray job: descriptor, zeroed counters, cancel flag cleared. It
+// enters the claim order at the next launch.
 cudaError_t publish(geon_server* S, HostJob* J, const ServeJob& sj) {
   const int slot = J->slot;
-  const int c = J->cls;
   S->h_jobs[slot] = sj;
-  S->h_ring_slot[slot] = slot;
   cudaError_t e = cudaMemcpyAsync(S->d_jobs + slot, S->h_jobs + slot, sizeof sj, cudaMemcpyHostToDevice, S->s_main);
   for (int k = 0; k < 3 && e == cudaSuccess; ++k)
     e = cudaMemsetAsync(S->d_counters + (size_t)k * SERVE_MAX_JOBS + slot, 0, sizeof(unsigned long long), S->s_main);
   if (e == cudaSuccess) e = cudaMemsetAsync(S->d_cancel + slot, 0, sizeof(unsigned), S->s_main);
-  const unsigned pos = S->h_tail[c];
-  S->h_tail[c] = pos + 1;
-  int* ring = S->d_rings + (size_t)c * SERVE_RING;
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(ring + (pos % SERVE_RING), S->h_ring_slot + slot, sizeof(int), cudaMemcpyHostToDevice,
-                        S->s_main);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&S->d_cls[c].tail, S->h_tail + c, sizeof(unsigned), cudaMemcpyHostToDevice, S->s_main);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(S->s_main);  // staging is reused by the next publish
-  S->h_counters[slot] = 0;
-  S->h_counters[SERVE_MAX_JOBS + slot] = 0;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(S->s_main);  // the descriptor staging is reused
+  for (int k = 0; k < 3; ++k) S->h_counters[(size_t)k * SERVE_MAX_JOBS + slot] = 0;
   J->tracing = true;
   return e;
+}
+
+// The claim order of every class for the next launch: jobs with unclaimed
+// rays, fewest unclaimed first (arrival order on ties), so a small request is
+// not queued behind a large one; rays already in flight continue first.
+void write_claim_order(geon_server* S) {
+  std::vector<std::pair<std::pair<int64_t, uint64_t>, int>> order[SERVE_CLASSES];
+  for (const HostJob* J : S->active) {
+    if (!J->tracing || J->stop_flagged) continue;
+    const int64_t claimed = (int64_t)S->h_counters[J->slot];
+    const int64_t left = J->nrays - (claimed < J->nrays ? claimed : J->nrays);
+    if (left > 0) order[J->cls].push_back({{left, J->id}, J->slot});
+  }
+  for (int c = 0; c < SERVE_CLASSES; ++c) {
+    std::sort(order[c].begin(), order[c].end());
+    int* dst = S->h_order + (size_t)c * SERVE_RING;
+    for (size_t i = 0; i < order[c].size(); ++i) dst[i] = order[c][i].second;
+    S->h_tail_head[2 * c] = (unsigned)order[c].size();
+    S->h_tail_head[2 * c + 1] = 0;
+  }
 }
 
 // Midpoints of the next `levels` halvings of [lo, hi] in heap order (node i at
@@ -558,6 +576,7 @@ void server_loop(geon_server* S) {
       continue;
     }
     // 4. one serving launch: prologue, class kernels, counter copy-back
+    write_claim_order(S);
     lk.unlock();
     note_launches(1 + SERVE_CLASSES);
     cudaError_t e = cudaGraphLaunch(S->graph, S->s_main);
@@ -579,9 +598,9 @@ void server_loop(geon_server* S) {
         }
         continue;
       }
-      const unsigned long long done = S->h_counters[J->slot];
+      const unsigned long long done = S->h_counters[SERVE_MAX_JOBS + J->slot];
       if ((int64_t)done < J->nrays) continue;
-      J->ray_steps += (double)S->h_counters[SERVE_MAX_JOBS + J->slot];
+      J->ray_steps += (double)S->h_counters[2 * SERVE_MAX_JOBS + J->slot];
       if (J->spec.type == GEON_JOB_RENDER) {
         J->tracing = false;
         hand_off(S, J);
@@ -740,22 +759,24 @@ int geon_server_create(size_t budget_bytes, geon_server_t* out) {
   if ((e = cudaMalloc(&S->d_counters, sizeof(unsigned long long) * 3 * SERVE_MAX_JOBS)) != cudaSuccess)
     return bad(e, "counters");
   if ((e = cudaMalloc(&S->d_cancel, sizeof(unsigned) * SERVE_MAX_JOBS)) != cudaSuccess) return bad(e, "flags");
-  if ((e = cudaMallocHost(&S->h_counters, sizeof(unsigned long long) * 2 * SERVE_MAX_JOBS)) != cudaSuccess)
+  if ((e = cudaMallocHost(&S->h_counters, sizeof(unsigned long long) * 3 * SERVE_MAX_JOBS)) != cudaSuccess)
     return bad(e, "pinned counters");
   if ((e = cudaMallocHost(&S->h_flags, sizeof(int) * SERVE_MAX_JOBS)) != cudaSuccess) return bad(e, "pinned flags");
   if ((e = cudaMallocHost(&S->h_jobs, sizeof(ServeJob) * SERVE_MAX_JOBS)) != cudaSuccess)
     return bad(e, "pinned job table");
-  if ((e = cudaMallocHost(&S->h_tail, sizeof(unsigned) * SERVE_CLASSES)) != cudaSuccess) return bad(e, "pinned tails");
-  if ((e = cudaMallocHost(&S->h_ring_slot, sizeof(int) * SERVE_MAX_JOBS)) != cudaSuccess)
-    return bad(e, "pinned ring staging");
+  if ((e = cudaMallocHost(&S->h_order, sizeof(int) * SERVE_RING * SERVE_CLASSES)) != cudaSuccess)
+    return bad(e, "pinned claim order");
+  if ((e = cudaMallocHost(&S->h_tail_head, sizeof(unsigned) * 2 * SERVE_CLASSES)) != cudaSuccess)
+    return bad(e, "pinned claim order length");
   if ((e = cudaMallocHost(&S->h_one, sizeof(unsigned))) != cudaSuccess) return bad(e, "pinned flag");
   if ((e = cudaMalloc(&S->d_rings, sizeof(int) * SERVE_RING * SERVE_CLASSES)) != cudaSuccess) return bad(e, "rings");
   if ((e = cudaMalloc(&S->d_resume, sizeof(ResumeEntry) * resume_total)) != cudaSuccess)
     return bad(e, "resume pools");
   if ((e = cudaMalloc(&S->d_epoch, sizeof(unsigned))) != cudaSuccess) return bad(e, "epoch");
   *S->h_one = 1u;
-  std::memset(S->h_tail, 0, sizeof(unsigned) * SERVE_CLASSES);
-  std::memset(S->h_counters, 0, sizeof(unsigned long long) * 2 * SERVE_MAX_JOBS);
+  std::memset(S->h_order, 0, sizeof(int) * SERVE_RING * SERVE_CLASSES);
+  std::memset(S->h_tail_head, 0, sizeof(unsigned) * 2 * SERVE_CLASSES);
+  std::memset(S->h_counters, 0, sizeof(unsigned long long) * 3 * SERVE_MAX_JOBS);
   std::memset(S->h_flags, 0, sizeof(int) * SERVE_MAX_JOBS);
   cudaMemset(S->d_counters, 0, sizeof(unsigned long long) * 3 * SERVE_MAX_JOBS);
   cudaMemset(S->d_cancel, 0, sizeof(unsigned) * SERVE_MAX_JOBS);
@@ -953,8 +974,8 @@ int geon_server_destroy(geon_server_t S) {
   cudaFree(S->d_cls);
   cudaFree(S->d_counters);
   cudaFree(S->d_cancel);
-  for (void* p : {(void*)S->h_counters, (void*)S->h_flags, (void*)S->h_jobs, (void*)S->h_tail,
-                  (void*)S->h_ring_slot, (void*)S->h_one})
+  for (void* p : {(void*)S->h_counters, (void*)S->h_flags, (void*)S->h_jobs, (void*)S->h_order,
+                  (void*)S->h_tail_head, (void*)S->h_one})
     if (p) cudaFreeHost(p);
   cudaFree(S->d_rings);
   cudaFree(S->d_resume);

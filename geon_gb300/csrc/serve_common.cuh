@@ -1,22 +1,23 @@
 // Device side of the serving engine (serve.cu): a work queue of ray jobs shared
 // by many requests, and the persistent kernel loop that drains it.
 //
-// Jobs of one class (metric kind x precision) are published in a ring; each
-// job holds a claim counter. A warp refills its idle lanes first from the
+// Each job holds a claim counter. Before every launch the host writes, per
+// class (metric kind x precision), the claim order: the jobs that still have
+// unclaimed rays, fewest first. A warp refills its idle lanes first from the
 // class's resume pool (rays interrupted at the end of the previous launch),
-// then from the jobs in ring order, one atomic per warp per job. A launch runs
+// then from the jobs in that order, one atomic per warp per job. A launch runs
 // a fixed number of warp iterations (one RK4 step each); rays still in flight
 // then write their state to the other resume buffer and are picked up by the
 // next launch, so ray state stays resident in HBM between launches and new
 // requests join at every launch (continuous batching). All loops are bounded:
-// the iteration budget, and the ring distance between head and tail.
+// the iteration budget, and the length of the claim order.
 #pragma once
 #include "trace_common.cuh"
 
 namespace geon {
 
-constexpr unsigned SERVE_RING = 65536;  // ring positions per class
-constexpr int SERVE_MAX_JOBS = 4096;    // job slots
+constexpr int SERVE_MAX_JOBS = 4096;              // job slots
+constexpr unsigned SERVE_RING = SERVE_MAX_JOBS;   // claim-order entries per class
 constexpr int SERVE_CLASSES = 8;        // 4 metric kinds x 2 precisions
 
 struct ServeJob {
@@ -42,8 +43,8 @@ struct ResumeEntry {
 };
 
 struct ServeClass {
-  unsigned tail;                         // ring positions published (host, between launches)
-  unsigned head;                         // ring positions fully claimed (kernels, atomicMax)
+  unsigned tail;                         // entries in the claim order (host, before each launch)
+  unsigned head;                         // entries fully claimed (host sets 0; kernels, atomicMax)
   unsigned long long resume_count[2];    // entries in each resume buffer
   unsigned long long resume_claim;       // entries of the input buffer taken this launch
   unsigned long long resume_cap;         // capacity of each buffer
@@ -98,8 +99,8 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
       }
       need = __ballot_sync(FULL, slot < 0);
     }
-    // one read of the shared head per warp: every lane must walk the same ring
-    // positions, since lane offsets are taken from the leader's claim
+    // one read of the shared head per warp: every lane must walk the same
+    // claim-order positions, since lane offsets are taken from the leader's claim
     unsigned pos = tail;
     if (jobs_open) {
       if (lane == 0) pos = atomicAdd(&cl->head, 0u);
