@@ -14,7 +14,7 @@ from .camera import Camera
 from .geodesic import FP64, MIXED, TraceResult, mom, pos, trace, trace_dev
 from .metric import (ALCUBIERRE, CAPTURED, DIVERGED, ESCAPED, MINKOWSKI, MORRIS_THORNE, SCHWARZSCHILD,
                      Alcubierre, Metric, Minkowski, MorrisThorne, Schwarzschild, from_kind)
-from .render import RenderConfig, RenderStats, render, tonemap, write_png
+from .render import RenderConfig, RenderStats, render, render_u8, tonemap, write_png
 from .serve import Job, Server
 
 

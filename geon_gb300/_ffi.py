@@ -61,7 +61,7 @@ class GeonJob(ctypes.Structure):
                 ("precision", ctypes.c_int32), ("deadline_s", ctypes.c_double),
                 ("camera", GeonCamera), ("render", GeonRenderConfig),
                 ("rgb", c_void_p), ("render_stats", c_void_p), ("pixel_class", c_void_p),
-                ("pixel_steps", c_void_p),
+                ("pixel_steps", c_void_p), ("rgb8", c_void_p),
                 ("r_obs", ctypes.c_double), ("lo", ctypes.c_double), ("hi", ctypes.c_double),
                 ("step", ctypes.c_double), ("max_steps", ctypes.c_int64), ("iters", ctypes.c_int32),
                 ("rays_per_round", ctypes.c_int32), ("alpha_c", c_void_p), ("lo_out", c_void_p),
@@ -104,6 +104,10 @@ SIGNATURES = {
                                               ctypes.c_double, c_double_p]),
     "geon_render": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonCamera), ctypes.POINTER(GeonRenderConfig),
                                    c_float_p, ctypes.POINTER(GeonRenderStats)]),
+    "geon_render_u8": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonCamera), ctypes.POINTER(GeonRenderConfig),
+                                      c_void_p, c_void_p, ctypes.POINTER(GeonRenderStats)]),
+    "geon_tonemap_u8": (ctypes.c_int, [c_void_p, c_size_t, c_void_p]),
+    "geon_tonemap_u8_dev": (ctypes.c_int, [c_void_p, c_size_t, c_void_p, c_void_p]),
     "geon_render_ex": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonCamera), ctypes.POINTER(GeonRenderConfig),
                                       c_float_p, ctypes.POINTER(GeonRenderStats), c_int32_p, c_int64_p]),
     "geon_sky_sample": (ctypes.c_int, [c_double_p, c_size_t, ctypes.c_int, c_float_p]),

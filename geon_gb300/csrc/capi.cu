@@ -545,10 +545,11 @@ int geon_camera_ray_states(const geon_camera* cam, const double tetrad[16], doub
   return GEON_OK;
 }
 
-int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
-                   geon_render_stats* stats, int32_t* pixel_class, int64_t* pixel_steps) {
+// render() with its f32 image (rgb) and/or write_png's tonemapped bytes (rgb8).
+static int render_any(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
+                      uint8_t* rgb8, geon_render_stats* stats, int32_t* pixel_class, int64_t* pixel_steps) {
   if (int rc = check_metric(m)) return rc;
-  if (!cfg || !rgb) return fail(GEON_ERR_INVALID, "null buffer");
+  if (!cfg || (!rgb && !rgb8)) return fail(GEON_ERR_INVALID, "null buffer");
   if (!valid_precision(cfg->precision)) return fail(GEON_ERR_INVALID, "unknown precision");
   if (cfg->max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
   cudaStream_t s = host_stream();
@@ -563,7 +564,7 @@ int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_co
   GEON_CUDA(dsteps.alloc(sizeof(int64_t) * nsamp, s));
   GEON_CUDA(dres.alloc(sizeof(double) * nsamp, s));
   GEON_CUDA(drgb.alloc(sizeof(float) * 3 * npix, s));
-  GEON_CUDA(dcls.alloc(sizeof(int32_t) * npix, s));
+  GEON_CUDA(dcls.alloc(sizeof(int32_t) * npix + (rgb8 ? 3 * npix : 0), s));  // + the bytes of rgb8
   GEON_CUDA(dpst.alloc(sizeof(int64_t) * npix, s));
   const size_t ws_bytes = sizeof(unsigned long long) * 8;
   GEON_CUDA(ws.alloc(ws_bytes, s));
@@ -586,11 +587,13 @@ int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_co
   unsigned long long* dstats = wsu + 2;  // 6 counters
   GEON_CUDA(launch_trace(L, cfg->precision, SRC_CAMERA, SINK_RENDER, s));
   counted();
+  uint8_t* d8 = rgb8 ? reinterpret_cast<uint8_t*>(dcls.as<int32_t>() + npix) : nullptr;
   GEON_CUDA(launch_render_reduce(dsrgb.as<float>(), dterm.as<int32_t>(), dsteps.as<int64_t>(),
-                                 dres.as<double>(), npix, spa, drgb.as<float>(), dcls.as<int32_t>(),
-                                 dpst.as<int64_t>(), dstats, s));
+                                 dres.as<double>(), npix, spa, rgb ? drgb.as<float>() : nullptr,
+                                 dcls.as<int32_t>(), dpst.as<int64_t>(), dstats, s, d8));
   unsigned long long hst[6];
-  GEON_CUDA(cudaMemcpyAsync(rgb, drgb.p, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, s));
+  if (rgb) GEON_CUDA(cudaMemcpyAsync(rgb, drgb.p, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, s));
+  if (rgb8) GEON_CUDA(cudaMemcpyAsync(rgb8, d8, 3 * npix, cudaMemcpyDeviceToHost, s));
   if (int rc = copy_out(pixel_class, dcls.p, sizeof(int32_t) * npix, s)) return rc;
   if (int rc = copy_out(pixel_steps, dpst.p, sizeof(int64_t) * npix, s)) return rc;
   GEON_CUDA(cudaMemcpyAsync(hst, dstats, sizeof hst, cudaMemcpyDeviceToHost, s));
@@ -609,9 +612,44 @@ int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_co
   return singular_status(flags);
 }
 
+int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
+                   geon_render_stats* stats, int32_t* pixel_class, int64_t* pixel_steps) {
+  if (!rgb) return fail(GEON_ERR_INVALID, "null buffer");
+  return render_any(m, cam, cfg, rgb, nullptr, stats, pixel_class, pixel_steps);
+}
+
 int geon_render(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, float* rgb,
                 geon_render_stats* stats) {
   return geon_render_ex(m, cam, cfg, rgb, stats, nullptr, nullptr);
+}
+
+int geon_render_u8(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg, uint8_t* rgb8,
+                   float* rgb, geon_render_stats* stats) {
+  if (!rgb8) return fail(GEON_ERR_INVALID, "null buffer");
+  return render_any(m, cam, cfg, rgb, rgb8, stats, nullptr, nullptr);
+}
+
+int geon_tonemap_u8_dev(const float* rgb, size_t n, uint8_t* out, void* stream) {
+  if (n == 0) return GEON_OK;
+  if (!rgb || !out) return fail(GEON_ERR_INVALID, "null buffer");
+  counted();
+  GEON_CUDA(launch_tonemap(rgb, (int64_t)n, out, static_cast<cudaStream_t>(stream)));
+  return GEON_OK;
+}
+
+int geon_tonemap_u8(const float* rgb, size_t n, uint8_t* out) {
+  if (n == 0) return GEON_OK;
+  if (!rgb || !out) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf d;
+  GEON_CUDA(d.alloc(sizeof(float) * n + n, s));
+  uint8_t* d8 = reinterpret_cast<uint8_t*>(d.as<float>() + n);
+  GEON_CUDA(cudaMemcpyAsync(d.p, rgb, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  counted();
+  GEON_CUDA(launch_tonemap(d.as<float>(), (int64_t)n, d8, s));
+  GEON_CUDA(cudaMemcpyAsync(out, d8, n, cudaMemcpyDeviceToHost, s));
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
 }
 
 int geon_sky_sample(const double* dir, size_t n, int show_stars, float* rgb) {

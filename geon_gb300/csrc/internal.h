@@ -88,10 +88,12 @@ struct TraceLaunch {
 cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 // ---- launchers (trace_mixed.cu) ----
 cudaError_t launch_trace_mixed(const TraceLaunch& L, int src, int sink, cudaStream_t s);
+// rgb and rgb8 (the tonemapped bytes) may each be null
 cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,
                                  const double* resid, int64_t npix, int64_t spa, float* rgb,
                                  int32_t* pclass, int64_t* psteps, unsigned long long* stats,
-                                 cudaStream_t s);
+                                 cudaStream_t s, uint8_t* rgb8 = nullptr);
+cudaError_t launch_tonemap(const float* rgb, int64_t n, uint8_t* out, cudaStream_t s);
 cudaError_t launch_pointwise(const MetricDesc& M, int what, const double* in, int64_t n, double* out,
                              int32_t* iout, int* flags, cudaStream_t s);
 cudaError_t launch_tetrad(const MetricDesc& M, const double* obs, double* out16, int* status,

@@ -117,6 +117,7 @@ struct RenderBufs {
   int32_t* pcls;
   int64_t* pst;
   unsigned long long* stats;
+  uint8_t* rgb8;
 };
 size_t render_bufs(char* base, int64_t nsamp, int64_t npix, RenderBufs* b) {
   Carve c(base);
@@ -129,6 +130,7 @@ size_t render_bufs(char* base, int64_t nsamp, int64_t npix, RenderBufs* b) {
   r.pcls = c.take<int32_t>(npix);
   r.pst = c.take<int64_t>(npix);
   r.stats = c.take<unsigned long long>(8);
+  r.rgb8 = c.take<uint8_t>(3 * npix);
   if (b) *b = r;
   return c.off;
 }
@@ -639,10 +641,13 @@ void finish_loop(geon_server* S) {
       e = cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s);
       note_launches(1);
       if (e == cudaSuccess)
-        e = launch_render_reduce(b.srgb, b.term, b.steps, b.resid, J->npix, J->spa, b.rgb, b.pcls, b.pst, b.stats, s);
+        e = launch_render_reduce(b.srgb, b.term, b.steps, b.resid, J->npix, J->spa, b.rgb, b.pcls, b.pst, b.stats, s,
+                                 q.rgb8 ? b.rgb8 : nullptr);
       unsigned long long st[6] = {};
-      if (e == cudaSuccess)
+      if (e == cudaSuccess && q.rgb)
         e = cudaMemcpyAsync(q.rgb, b.rgb, sizeof(float) * 3 * J->npix, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess && q.rgb8)
+        e = cudaMemcpyAsync(q.rgb8, b.rgb8, 3 * J->npix, cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess && q.pixel_class)
         e = cudaMemcpyAsync(q.pixel_class, b.pcls, sizeof(int32_t) * J->npix, cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess && q.pixel_steps)
@@ -711,7 +716,7 @@ int validate(const geon_job* j) {
     if (j->camera.forward_sign != 1 && j->camera.forward_sign != -1)
       return set_last_error(GEON_ERR_INVALID, "forward_sign must be +1 or -1");
     if (j->render.max_steps < 0) return set_last_error(GEON_ERR_INVALID, "max_steps < 0");
-    if (!j->rgb) return set_last_error(GEON_ERR_INVALID, "null buffer");
+    if (!j->rgb && !j->rgb8) return set_last_error(GEON_ERR_INVALID, "null buffer");
   } else if (j->type == GEON_JOB_BISECT) {
     if (j->metric_kind != GEON_SCHWARZSCHILD)
       return set_last_error(GEON_ERR_INVALID, "shadow bisection needs a Schwarzschild metric");

@@ -170,11 +170,40 @@ cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStrea
 // stats: [captured, escaped, diverged, sum of per-pixel step averages,
 //         max residual bits, sum of all sample steps]
 // ---------------------------------------------------------------------------
+// write_png's tonemap (render.rs:174-178): clamp to [0, 1] (NaN passes
+// through, as f32::clamp does), raise to the f32 power 1/2.2, scale by 255,
+// round half away from zero and cast with saturation (NaN -> 0). The power is
+// evaluated in FP64 and rounded once to f32; over every f32 in [0, 1] this
+// gives the same byte as glibc's powf (checked exhaustively on the host).
+__device__ __forceinline__ uint8_t tonemap_u8(float c) {
+  float v = c;
+  if (v < 0.0f) v = 0.0f;
+  if (v > 1.0f) v = 1.0f;
+  const float gamma_inv = 1.0f / 2.2f;
+  const float p = __double2float_rn(pow((double)v, (double)gamma_inv));
+  const float y = roundf(p * 255.0f);
+  if (!(y > 0.0f)) return 0;
+  if (y >= 255.0f) return 255;
+  return (uint8_t)y;
+}
+
+__global__ void tonemap_kernel(const float* __restrict__ rgb, int64_t n, uint8_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = tonemap_u8(rgb[i]);
+}
+
+cudaError_t launch_tonemap(const float* rgb, int64_t n, uint8_t* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int block = 256;
+  tonemap_kernel<<<(unsigned)((n + block - 1) / block), block, 0, s>>>(rgb, n, out);
+  return cudaGetLastError();
+}
+
 __global__ void render_reduce_kernel(const float* __restrict__ srgb, const int32_t* __restrict__ term,
                                      const int64_t* __restrict__ steps, const double* __restrict__ resid,
                                      int64_t npix, int64_t spa, float* __restrict__ rgb,
                                      int32_t* __restrict__ pclass, int64_t* __restrict__ psteps,
-                                     unsigned long long* __restrict__ stats) {
+                                     unsigned long long* __restrict__ stats, uint8_t* __restrict__ rgb8) {
   const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int c_cap = 0, c_esc = 0, c_div = 0;
   unsigned long long pst = 0, tot = 0, rbits = 0;
@@ -198,9 +227,17 @@ __global__ void render_reduce_kernel(const float* __restrict__ srgb, const int32
       if (isfinite(r) && r > maxr) maxr = r;
     }
     const float nf = (float)spa2;
-    rgb[3 * pix] = acc0 / nf;
-    rgb[3 * pix + 1] = acc1 / nf;
-    rgb[3 * pix + 2] = acc2 / nf;
+    const float o0 = acc0 / nf, o1 = acc1 / nf, o2 = acc2 / nf;
+    if (rgb) {
+      rgb[3 * pix] = o0;
+      rgb[3 * pix + 1] = o1;
+      rgb[3 * pix + 2] = o2;
+    }
+    if (rgb8) {
+      rgb8[3 * pix] = tonemap_u8(o0);
+      rgb8[3 * pix + 1] = tonemap_u8(o1);
+      rgb8[3 * pix + 2] = tonemap_u8(o2);
+    }
     int cls;
     if (nd > 0 && nd >= nc && nd >= ne) cls = TERM_DIVERGED;
     else if (nc >= ne) cls = TERM_CAPTURED;
@@ -239,12 +276,12 @@ __global__ void render_reduce_kernel(const float* __restrict__ srgb, const int32
 cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,
                                  const double* resid, int64_t npix, int64_t spa, float* rgb,
                                  int32_t* pclass, int64_t* psteps, unsigned long long* stats,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, uint8_t* rgb8) {
   if (npix <= 0) return cudaSuccess;
   const int block = 256;
   const int64_t grid = (npix + block - 1) / block;
   render_reduce_kernel<<<(unsigned)grid, block, 0, s>>>(srgb, term, steps, resid, npix, spa, rgb,
-                                                        pclass, psteps, stats);
+                                                        pclass, psteps, stats, rgb8);
   return cudaGetLastError();
 }
 

@@ -62,15 +62,33 @@ def render(metric, camera, cfg=None, with_classes=False):
     return rgb, stats
 
 
+def render_u8(metric, camera, cfg=None, with_float=False):
+    """render() followed by write_png's tonemap on the GPU: (height, width, 3)
+    uint8, the bytes write_png encodes [+ the float image], and RenderStats."""
+    cfg = cfg or RenderConfig()
+    rgb8 = np.empty((camera.height, camera.width, 3), dtype=np.uint8)
+    rgb = np.empty((camera.height, camera.width, 3), dtype=np.float32) if with_float else None
+    st = _ffi.GeonRenderStats()
+    check(_ffi.load().geon_render_u8(metric.handle, camera.c_struct(), cfg.c_struct(), rgb8.ctypes.data,
+                                     rgb.ctypes.data if rgb is not None else None, st))
+    stats = RenderStats(st.captured, st.escaped, st.diverged, st.max_null_residual, st.avg_steps,
+                        st.total_steps)
+    return (rgb8, rgb, stats) if with_float else (rgb8, stats)
+
+
 def tonemap(pixels):
-    """write_png's tonemap (render.rs:169-183): clamp, gamma 1/2.2, round to u8."""
-    v = np.clip(np.asarray(pixels, dtype=np.float32), 0.0, 1.0) ** np.float32(1.0 / 2.2)
-    return np.round(v * np.float32(255.0)).astype(np.uint8)
+    """write_png's tonemap (render.rs:169-183) on the GPU: clamp, ^(1/2.2), *255, round to u8."""
+    a = np.ascontiguousarray(pixels, dtype=np.float32)
+    out = np.empty(a.shape, dtype=np.uint8)
+    check(_ffi.load().geon_tonemap_u8(a.ctypes.data, a.size, out.ctypes.data))
+    return out
 
 
 def write_png(path, pixels, width, height):
-    """Tonemap and write an RGB PNG (host side, like the reference's image crate call)."""
-    img = tonemap(pixels).reshape(height, width, 3)
+    """Write an RGB PNG (host side, like the reference's image crate call). pixels:
+    the float image (tonemapped on the GPU) or the uint8 bytes of render_u8."""
+    px = np.asarray(pixels)
+    img = (px if px.dtype == np.uint8 else tonemap(px)).reshape(height, width, 3)
     raw = b"".join(b"\x00" + img[j].tobytes() for j in range(height))
 
     def chunk(tag, data):

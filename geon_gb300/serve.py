@@ -63,6 +63,8 @@ class Job:
             st = o["stats"]
             stats = RenderStats(st.captured, st.escaped, st.diverged, st.max_null_residual, st.avg_steps,
                                 st.total_steps)
+            if "rgb8" in o:
+                return o["rgb"], stats, o["cls"], o["steps"], o["rgb8"]
             return o["rgb"], stats, o["cls"], o["steps"]
         if self.kind == JOB_BISECT:
             return {"alpha_c": float(o["v"][0]), "lo": float(o["v"][1]), "hi": float(o["v"][2]),
@@ -98,8 +100,9 @@ class Server:
         check(self._lib.geon_server_submit(self._h, ctypes.byref(job), ctypes.byref(jid)))
         return Job(self, jid.value, kind, job, outputs)
 
-    def submit_render(self, metric, camera, cfg=None, precision=None, deadline_s=0.0):
-        """render.render(metric, camera, cfg, with_classes=True) as a request."""
+    def submit_render(self, metric, camera, cfg=None, precision=None, deadline_s=0.0, with_u8=False):
+        """render.render(metric, camera, cfg, with_classes=True) as a request
+        (with_u8: also the tonemapped bytes of render_u8, returned fifth)."""
         cfg = cfg or RenderConfig()
         job = _ffi.GeonJob()
         job.type = JOB_RENDER
@@ -116,6 +119,9 @@ class Server:
         job.pixel_class = _addr(out["cls"])
         job.pixel_steps = _addr(out["steps"])
         job.render_stats = ctypes.addressof(out["stats"])
+        if with_u8:
+            out["rgb8"] = np.empty((camera.height, camera.width, 3), dtype=np.uint8)
+            job.rgb8 = _addr(out["rgb8"])
         return self._submit(job, JOB_RENDER, out)
 
     def submit_bisect(self, metric, r_obs, lo, hi, iters=60, step=0.01, max_steps=200000, precision="fp64",

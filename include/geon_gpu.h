@@ -151,6 +151,15 @@ int geon_render(geon_metric_t m, const geon_camera* cam, const geon_render_confi
 int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg,
                    float* rgb, geon_render_stats* stats, int32_t* pixel_class,
                    int64_t* pixel_steps);
+/* render() followed by write_png's tonemap (render.rs:169-183) on the device:
+ * rgb8 receives width*height*3 bytes, the buffer write_png hands to the PNG
+ * encoder (clamp to [0, 1], ^(1/2.2) in f32, *255, round, saturating cast).
+ * rgb (the f32 image) may be NULL. */
+int geon_render_u8(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg,
+                   uint8_t* rgb8, float* rgb, geon_render_stats* stats);
+/* write_png's tonemap (render.rs:174-178) alone, over n floats. */
+int geon_tonemap_u8(const float* rgb, size_t n, uint8_t* out);
+int geon_tonemap_u8_dev(const float* rgb, size_t n, uint8_t* out, void* stream);
 /* sky::sample (sky.rs:107-120) over n unit directions (n*3 in, n*3 out). */
 int geon_sky_sample(const double* dir, size_t n, int show_stars, float* rgb);
 /* sky::SHOW_STARS (sky.rs:23; set by bin/render.rs:71-73). */
@@ -284,10 +293,11 @@ typedef struct {
   /* GEON_JOB_RENDER: geon_render_ex's arguments (render.precision is ignored) */
   geon_camera camera;
   geon_render_config render;
-  float* rgb;                     /* out: width*height*3 */
+  float* rgb;                     /* out: width*height*3 (may be NULL when rgb8 is set) */
   geon_render_stats* render_stats;/* out, may be NULL */
   int32_t* pixel_class;           /* out, may be NULL */
   int64_t* pixel_steps;           /* out, may be NULL */
+  uint8_t* rgb8;                  /* out, may be NULL: the tonemapped bytes (geon_render_u8) */
   /* GEON_JOB_BISECT: one bracket of geon_shadow_bisect (Schwarzschild only) */
   double r_obs, lo, hi, step;
   int64_t max_steps;

@@ -1032,6 +1032,21 @@ void orc_sky_sample(const double* dir3, int64_t n, int show_stars, float* rgb_ou
   for (int64_t i = 0; i < n; ++i) sky_sample(dir3 + 3 * i, show_stars != 0, rgb_out + 3 * i);
 }
 
+// render.rs:169-183 (write_png): `c.clamp(0.0, 1.0).powf(1.0 / 2.2)` in f32,
+// then `(v * 255.0).round() as u8` (round half away from zero; the cast
+// saturates and maps NaN to 0).
+void orc_tonemap_u8(const float* rgb, int64_t n, uint8_t* out) {
+  const float gamma_inv = 1.0f / 2.2f;
+  for (int64_t i = 0; i < n; ++i) {
+    float v = rgb[i];
+    if (v < 0.0f) v = 0.0f;
+    if (v > 1.0f) v = 1.0f;
+    const float p = powf(v, gamma_inv);
+    const float y = roundf(p * 255.0f);
+    out[i] = !(y > 0.0f) ? 0 : (y >= 255.0f ? 255 : (uint8_t)y);
+  }
+}
+
 // render.rs:55-166
 int orc_render(int kind, const double* params, int math, const double* observer, double fov_y_deg,
                int64_t width, int64_t height, int64_t row0, int64_t nrows, double step,

@@ -85,6 +85,10 @@ int orc_render(int kind, const double* params, int math, const double* observer,
                int nthreads, float* rgb_out, int32_t* pclass_out, int64_t* psteps_out,
                orc_render_stats* stats);
 
+/* write_png's tonemap (render.rs:174-178): clamp, f32 powf(v, 1/2.2) from libm,
+   *255, round, saturating cast to u8 (NaN -> 0). */
+void orc_tonemap_u8(const float* rgb, int64_t n, uint8_t* out);
+
 /* curvature.rs. what: 0 riemann(256) 1 ricci(16) 2 ricci_scalar(1) 3 einstein(16)
    4 stress_energy(16). faithful=1 evaluates exactly the reference's call graph
    (Riemann recomputed inside ricci_scalar); 0 computes it once (bit-identical). */

@@ -189,6 +189,14 @@ def render(kind, params, observer, fov_y_deg, width, height, step=0.05, max_step
     return rgb, cls, pst, st.as_dict()
 
 
+def tonemap_u8(rgb):
+    """write_png's tonemap (render.rs:174-178) with libm powf."""
+    a = np.ascontiguousarray(rgb, dtype=np.float32)
+    out = np.empty(a.shape, dtype=np.uint8)
+    lib().orc_tonemap_u8(_p(a, ctypes.c_float), ctypes.c_int64(a.size), _p(out, ctypes.c_uint8))
+    return out
+
+
 WHAT = {"riemann": (0, 256), "ricci": (1, 16), "ricci_scalar": (2, 1), "einstein": (3, 16),
         "stress_energy": (4, 16)}
 

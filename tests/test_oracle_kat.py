@@ -116,3 +116,13 @@ def test_faithful_curvature_equals_single_riemann(orc):
     a = orc.nec(2, [2.0, 0.5, 2.0, 0.0], x, k, math=0, faithful=True)
     b = orc.nec(2, [2.0, 0.5, 2.0, 0.0], x, k, math=0, faithful=False)
     assert np.array_equal(a, b)
+
+
+def test_oracle_tonemap_known_values(orc):
+    """write_png's tonemap (render.rs:174-178): clamp, ^(1/2.2) in f32, *255, round, saturating cast."""
+    x = np.array([0.0, 1.0, 0.5, -1.0, 2.0, np.nan, np.inf, -np.inf, 0.214, 1e-30], dtype=np.float32)
+    assert orc.tonemap_u8(x).tolist() == [0, 255, 186, 0, 255, 0, 255, 0, 127, 0]
+    # every byte value is reached, monotonically, over [0, 1]
+    v = np.linspace(0.0, 1.0, 100001, dtype=np.float32)
+    t = orc.tonemap_u8(v)
+    assert np.all(np.diff(t.astype(int)) >= 0) and set(t.tolist()) == set(range(256))
