@@ -7,7 +7,7 @@ chain. The compute runs in hand-written sm_103a CUDA behind the C ABI of
 include/geon_gpu.h; this package is the Python host side of that ABI. There is
 no CPU fallback: without the built library every call raises.
 """
-from . import autotune, curvature, shadow, sky
+from . import autotune, curvature, energy, shadow, sky
 from ._ffi import load as _load
 from ._util import GeonError
 from .camera import Camera

@@ -29,6 +29,7 @@ UNITS = [
     ("capi.cu", ["--fmad=false"]),
     ("noalloc.cu", ["--fmad=false"]),
     ("serve.cu", ["--fmad=false"]),
+    ("energy.cu", ["--fmad=false"]),
 ]
 
 

@@ -226,6 +226,16 @@ int geon_curvature_grid_dev(geon_metric_t m, const geon_grid* grid, size_t nk, u
 int geon_wec_contraction(geon_metric_t m, const double* x, size_t n, const double* u, size_t nu,
                          int u_shared, double* out);
 
+/* --- bin/energy_conditions.rs (energy_conditions.rs:37-156) as one batched job --
+ * The 99 numbers the bin prints, in its order: Minkowski T(k,k), R; for
+ * Schwarzschild r = 5, 10, 30: T(k,k), R; Alcubierre (R 2, thickness 0.5, v 2):
+ * T(k,k) at the 41 scan points x = -4 + 0.2 n, the minimum, its x, the
+ * negative-part integral over x = -5 .. 5 (dx 0.05, the bin's accumulated
+ * positions); Morris-Thorne (b0 1): T(k,k) at the 41 points l = -4 + 0.2 n,
+ * the minimum, its l, then T^mu_nu[i][i] at the throat for i = 0..3. */
+#define GEON_ENERGY_CONDITIONS_N 99
+int geon_energy_conditions(double* out);
+
 /* --- shadow validation (bin/validate_shadow.rs:20-94) ------------------------ */
 /* equatorial_ray (validate_shadow.rs:20-35): n launch angles -> n States. */
 int geon_equatorial_rays(geon_metric_t schwarzschild, double r_obs, const double* alpha, size_t n,

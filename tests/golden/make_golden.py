@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures from the reference's own printed results.
 
 Reads, as text, the known-answer output the reference commits
-(docs/energy_conditions.txt, the stdout of bin/energy_conditions.rs) and the
+(docs/energy_conditions.txt, the stdout of bin/energy_conditions.rs, kept both
+as parsed values and line for line) and the
 shadow-validation lines of its README (README.md:43-45, the stdout of
 bin/validate_shadow.rs), and writes them as JSON next to this script. Run in a
 checkout where the reference sits at REFERENCE (default /root/reference); the
@@ -67,10 +68,17 @@ def shadow():
             "rel_err": float(e.group(1)), "minkowski_null_residual_order": float(nr.group(1))}
 
 
+def energy_conditions_stdout():
+    # the bin's stdout as the reference committed it, line for line
+    return open(os.path.join(REF, "docs", "energy_conditions.txt"), encoding="utf-8").read().splitlines()
+
+
 def main():
     ec = energy_conditions()
     sh = shadow()
-    for name, obj in (("energy_conditions.json", ec), ("validate_shadow.json", sh)):
+    for name, obj in (("energy_conditions.json", ec), ("validate_shadow.json", sh),
+                      ("energy_conditions_stdout.json", {"source": "docs/energy_conditions.txt",
+                                                         "lines": energy_conditions_stdout()})):
         with open(os.path.join(HERE, name), "w", encoding="utf-8") as f:
             json.dump(obj, f, indent=1, ensure_ascii=False)
             f.write("\n")

@@ -126,3 +126,16 @@ def test_oracle_tonemap_known_values(orc):
     v = np.linspace(0.0, 1.0, 100001, dtype=np.float32)
     t = orc.tonemap_u8(v)
     assert np.all(np.diff(t.astype(int)) >= 0) and set(t.tolist()) == set(range(256))
+
+
+def test_energy_conditions_report_format(orc):
+    """The report formatter (geon_gb300/energy.py) on the oracle's numbers gives the
+    reference's committed stdout of bin/energy_conditions.rs, line for line, in the
+    libm mode and in the deterministic-math mode the GPU shares."""
+    import json
+    import os
+    from geon_gb300 import energy
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "energy_conditions_stdout.json"),
+                          encoding="utf-8"))["lines"]
+    for math in (orc.LIBM, orc.GEON):
+        assert energy.report(orc.energy_conditions(math)) == gold
