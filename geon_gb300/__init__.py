@@ -11,7 +11,8 @@ from . import autotune, curvature, energy, shadow, sky
 from ._ffi import load as _load
 from ._util import GeonError
 from .camera import Camera
-from .geodesic import FP64, MIXED, TraceResult, mom, pos, trace, trace_dev
+from .geodesic import (ADAPTIVE, FP64, MIXED, TraceResult, adaptive_tolerance, mom, pos, set_adaptive_tolerance,
+                       trace, trace_dev)
 from .metric import (ALCUBIERRE, CAPTURED, DIVERGED, ESCAPED, MINKOWSKI, MORRIS_THORNE, SCHWARZSCHILD,
                      Alcubierre, Metric, Minkowski, MorrisThorne, Schwarzschild, from_kind)
 from .render import RenderConfig, RenderStats, render, render_u8, tonemap, write_png

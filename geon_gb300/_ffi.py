@@ -157,6 +157,8 @@ SIGNATURES = {
     "geon_server_stats_get": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonServerStats)]),
     "geon_server_destroy": (ctypes.c_int, [c_void_p]),
     "geon_energy_conditions": (ctypes.c_int, [c_double_p]),
+    "geon_set_adaptive_tolerance": (ctypes.c_int, [ctypes.c_double, ctypes.c_double]),
+    "geon_get_adaptive_tolerance": (None, [c_double_p, c_double_p]),
     "geon_launch_count": (ctypes.c_ulonglong, []),
     "geon_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, c_double_p]),
 }

@@ -25,6 +25,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
 UNITS = [
     ("trace_fp64.cu", ["--fmad=false"]),
     ("trace_mixed.cu", ["--fmad=false"]),
+    ("trace_adaptive.cu", ["--fmad=false"]),
     ("curvature_fp64.cu", ["--fmad=false"]),
     ("capi.cu", ["--fmad=false"]),
     ("noalloc.cu", ["--fmad=false"]),

@@ -29,6 +29,8 @@ std::atomic<int> g_show_stars{1};
 std::atomic<float> g_band[4] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
 std::atomic<int> g_reproject{0};
 std::atomic<int> g_reserve{0};
+std::atomic<double> g_rtol{1e-10};  // GEON_ADAPTIVE error tolerances
+std::atomic<double> g_atol{1e-12};
 // Mixed-kernel variant per metric kind and ray source (camera/array, equatorial),
 // chosen by geon_autotune_mixed (default 0).
 std::atomic<int> g_variant[4][2] = {{{0}, {0}}, {{0}, {0}}, {{0}, {0}}, {{0}, {0}}};
@@ -140,6 +142,8 @@ TraceLaunch base_launch(geon_metric_t m, double step, int64_t max_steps) {
   L.mixed_flags = g_reproject.load() ? MIXED_REPROJECT : 0;
   L.reserve_per_sm = g_reserve.load();
   L.variant = g_variant[m->desc.kind][0].load();
+  L.rtol = g_rtol.load();
+  L.atol = g_atol.load();
   return L;
 }
 
@@ -147,10 +151,12 @@ cudaError_t launch_trace(const TraceLaunch& L0, int precision, int src, int sink
   if (L0.n > 0) counted();
   TraceLaunch L = L0;
   if (src == SRC_EQUATORIAL) L.variant = g_variant[L.M.kind][1].load();
-  return precision == GEON_MIXED ? launch_trace_mixed(L, src, sink, s) : launch_trace_fp64(L, src, sink, s);
+  if (precision == GEON_MIXED) return launch_trace_mixed(L, src, sink, s);
+  if (precision == GEON_ADAPTIVE) return launch_trace_adaptive(L, src, sink, s);
+  return launch_trace_fp64(L, src, sink, s);
 }
 
-bool valid_precision(int p) { return p == GEON_FP64 || p == GEON_MIXED; }
+bool valid_precision(int p) { return p == GEON_FP64 || p == GEON_MIXED || p == GEON_ADAPTIVE; }
 
 // Levels of the speculative bisection tree traced per round: as many as keep
 // nb * (2^L - 1) launch angles within 16384 rays (at most 16).
@@ -227,6 +233,20 @@ double geon_get_mixed_band(int kind) {
 }
 
 void geon_set_mixed_reproject(int on) { g_reproject.store(on ? 1 : 0); }
+
+int geon_set_adaptive_tolerance(double rtol, double atol) {
+  if (!(rtol >= 0.0) || !(atol >= 0.0) || (rtol == 0.0 && atol == 0.0) || !std::isfinite(rtol) ||
+      !std::isfinite(atol))
+    return fail(GEON_ERR_INVALID, "bad tolerances");
+  g_rtol.store(rtol);
+  g_atol.store(atol);
+  return GEON_OK;
+}
+
+void geon_get_adaptive_tolerance(double* rtol, double* atol) {
+  if (rtol) *rtol = g_rtol.load();
+  if (atol) *atol = g_atol.load();
+}
 
 void geon_set_persistent_reserve(int blocks_per_sm) { g_reserve.store(blocks_per_sm < 0 ? 0 : blocks_per_sm); }
 

@@ -79,6 +79,8 @@ struct TraceLaunch {
   int reserve_per_sm;  // persistent grid leaves this many blocks per SM free
   int variant;         // mixed kernel register-cap variant (0: none, 1: 5 blocks/SM, 2: 6)
   int mixed_flags;     // MIXED_* bits
+  // adaptive stepping (GEON_ADAPTIVE): error tolerances
+  double rtol, atol;
   // work queue
   unsigned long long* queue;  // next unclaimed ray index
   int* flags;                 // bit 0: a metric became singular (inverse of g failed)
@@ -88,6 +90,8 @@ struct TraceLaunch {
 cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 // ---- launchers (trace_mixed.cu) ----
 cudaError_t launch_trace_mixed(const TraceLaunch& L, int src, int sink, cudaStream_t s);
+// ---- launchers (trace_adaptive.cu) ----
+cudaError_t launch_trace_adaptive(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 // rgb and rgb8 (the tonemapped bytes) may each be null
 cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,
                                  const double* resid, int64_t npix, int64_t spa, float* rgb,

@@ -77,7 +77,8 @@ extern "C" int geon_shadow_bisect_dev_noalloc(geon_metric_t m, double r_obs, con
   const MetricDesc* d = metric_desc(m);
   if (!d) return set_last_error(GEON_ERR_INVALID, "null metric handle");
   if (d->kind != GEON_SCHWARZSCHILD) return set_last_error(GEON_ERR_INVALID, "shadow bisection needs a Schwarzschild metric");
-  if (precision != GEON_FP64 && precision != GEON_MIXED) return set_last_error(GEON_ERR_INVALID, "unknown precision");
+  if (precision != GEON_FP64 && precision != GEON_MIXED && precision != GEON_ADAPTIVE)
+    return set_last_error(GEON_ERR_INVALID, "unknown precision");
   if (nb == 0) return GEON_OK;
   if (nb > NOALLOC_MAX_BRACKETS)
     return set_last_error(GEON_ERR_INVALID,

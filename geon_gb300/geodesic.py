@@ -6,8 +6,19 @@ import numpy as np
 from . import _ffi
 from ._util import check, dp, f64, i32p, i64p, points
 
-FP64, MIXED = 0, 1
-PRECISION = {"fp64": FP64, "mixed": MIXED, FP64: FP64, MIXED: MIXED}
+FP64, MIXED, ADAPTIVE = 0, 1, 2
+PRECISION = {"fp64": FP64, "mixed": MIXED, "adaptive": ADAPTIVE, FP64: FP64, MIXED: MIXED, ADAPTIVE: ADAPTIVE}
+
+
+def set_adaptive_tolerance(rtol, atol):
+    """Error tolerances of precision="adaptive" (FP64 Dormand-Prince 5(4))."""
+    check(_ffi.load().geon_set_adaptive_tolerance(float(rtol), float(atol)))
+
+
+def adaptive_tolerance():
+    r, a = _ffi.ctypes.c_double(), _ffi.ctypes.c_double()
+    _ffi.load().geon_get_adaptive_tolerance(_ffi.ctypes.byref(r), _ffi.ctypes.byref(a))
+    return r.value, a.value
 
 
 @dataclass

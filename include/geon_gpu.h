@@ -59,7 +59,11 @@ enum geon_metric_kind {
   GEON_MORRIS_THORNE = 3  /* metric/morris_thorne.rs */
 };
 enum geon_termination { GEON_DIVERGED = 0, GEON_CAPTURED = 1, GEON_ESCAPED = 2 };
-enum geon_precision { GEON_FP64 = 0, GEON_MIXED = 1 };
+/* GEON_ADAPTIVE (an extension; the reference lists it as a TODO at
+ * integrator.rs:5-7): FP64 Dormand-Prince 5(4) with error control instead of
+ * the fixed-step RK4; `step` is the first trial step, max_steps caps accepted
+ * steps, tolerances from geon_set_adaptive_tolerance. Not for the server. */
+enum geon_precision { GEON_FP64 = 0, GEON_MIXED = 1, GEON_ADAPTIVE = 2 };
 
 typedef struct geon_metric* geon_metric_t;
 
@@ -175,6 +179,11 @@ int geon_get_show_stars(void);
 int geon_set_mixed_band(int kind, double band);
 double geon_get_mixed_band(int kind);
 void geon_set_mixed_reproject(int on);
+/* Error tolerances of GEON_ADAPTIVE: a step is accepted when
+ * sqrt(mean_i((e_i / (atol + rtol * max(|y_i|, |y_new_i|)))^2)) <= 1.
+ * Defaults rtol 1e-10, atol 1e-12. Calls made after this use them. */
+int geon_set_adaptive_tolerance(double rtol, double atol);
+void geon_get_adaptive_tolerance(double* rtol, double* atol);
 /* Trace kernels are persistent (one grid fills every SM and pulls rays from a
  * device work queue). To let another job run beside one (e.g. bisections next
  * to a sweep), calls made after this keep `blocks_per_sm` resident slots per SM

@@ -551,6 +551,104 @@ TraceResult trace(const Met& metric, const State& y0, double step, int64_t max_s
   return TraceResult{DIVERGED, y, max_steps, std::fabs(dot4(g, p, p))};
 }
 
+// Adaptive stepping, the restatement of the GPU's GEON_ADAPTIVE mode (not a
+// reference feature: integrator.rs:5-7 lists it as a TODO). Dormand & Prince
+// 5(4) (J. Comput. Appl. Math. 6 (1980) 19-26) with first-same-as-last reuse,
+// the Hairer-Norsett-Wanner RMS error norm and a controller made of IEEE
+// operations only: accept when err <= 1, next h = h * clamp(0.9 / sqrt(sqrt(err)),
+// 0.2, 5); a non-finite trial is a rejection; 64 consecutive rejections end the
+// ray Diverged; max_steps counts accepted steps. Every expression keeps the
+// GPU's evaluation order, so both give the same bits.
+namespace dp5 {
+constexpr double A21 = 1.0 / 5.0;
+constexpr double A31 = 3.0 / 40.0, A32 = 9.0 / 40.0;
+constexpr double A41 = 44.0 / 45.0, A42 = -56.0 / 15.0, A43 = 32.0 / 9.0;
+constexpr double A51 = 19372.0 / 6561.0, A52 = -25360.0 / 2187.0, A53 = 64448.0 / 6561.0, A54 = -212.0 / 729.0;
+constexpr double A61 = 9017.0 / 3168.0, A62 = -355.0 / 33.0, A63 = 46732.0 / 5247.0, A64 = 49.0 / 176.0,
+                 A65 = -5103.0 / 18656.0;
+constexpr double B1 = 35.0 / 384.0, B3 = 500.0 / 1113.0, B4 = 125.0 / 192.0, B5 = -2187.0 / 6784.0,
+                 B6 = 11.0 / 84.0;
+constexpr double E1 = 71.0 / 57600.0, E3 = -71.0 / 16695.0, E4 = 71.0 / 1920.0, E5 = -17253.0 / 339200.0,
+                 E6 = 22.0 / 525.0, E7 = -1.0 / 40.0;
+constexpr int MAX_REJECT = 64;
+}  // namespace dp5
+
+template <class Met>
+TraceResult trace_adaptive(const Met& metric, const State& y0, double h0, int64_t max_steps, double rtol,
+                           double atol) {
+  using namespace dp5;
+  State y = y0, k1;
+  bool fresh = true;
+  double h = h0;
+  auto result = [&](int reason, int64_t n) {
+    const Vec4 x = pos(y);
+    const Mat4 g = metric.g(x);
+    const Vec4 p = mom(y);
+    return TraceResult{reason, y, n, std::fabs(dot4(g, p, p))};
+  };
+  for (int64_t n = 0; n < max_steps; ++n) {
+    const int reason = metric.terminate(pos(y));
+    if (reason != NONE) return result(reason, n);
+    if (fresh) {
+      k1 = rhs(metric, y);
+      fresh = false;
+    }
+    bool accepted = false;
+    for (int attempt = 0; attempt < MAX_REJECT && !accepted; ++attempt) {
+      State ys, yn;
+      for (int i = 0; i < 8; ++i) ys.y[i] = y.y[i] + h * (A21 * k1.y[i]);
+      const State k2 = rhs(metric, ys);
+      for (int i = 0; i < 8; ++i) ys.y[i] = y.y[i] + h * (A31 * k1.y[i] + A32 * k2.y[i]);
+      const State k3 = rhs(metric, ys);
+      for (int i = 0; i < 8; ++i) ys.y[i] = y.y[i] + h * ((A41 * k1.y[i] + A42 * k2.y[i]) + A43 * k3.y[i]);
+      const State k4 = rhs(metric, ys);
+      for (int i = 0; i < 8; ++i)
+        ys.y[i] = y.y[i] + h * (((A51 * k1.y[i] + A52 * k2.y[i]) + A53 * k3.y[i]) + A54 * k4.y[i]);
+      const State k5 = rhs(metric, ys);
+      for (int i = 0; i < 8; ++i)
+        ys.y[i] = y.y[i] + h * ((((A61 * k1.y[i] + A62 * k2.y[i]) + A63 * k3.y[i]) + A64 * k4.y[i]) +
+                                A65 * k5.y[i]);
+      const State k6 = rhs(metric, ys);
+      for (int i = 0; i < 8; ++i)
+        yn.y[i] = y.y[i] + h * ((((B1 * k1.y[i] + B3 * k3.y[i]) + B4 * k4.y[i]) + B5 * k5.y[i]) + B6 * k6.y[i]);
+      const State k7 = rhs(metric, yn);
+      double sum = 0.0;
+      bool finite = true;
+      for (int i = 0; i < 8; ++i) {
+        const double e = h * (((((E1 * k1.y[i] + E3 * k3.y[i]) + E4 * k4.y[i]) + E5 * k5.y[i]) + E6 * k6.y[i]) +
+                              E7 * k7.y[i]);
+        const double ay = std::fabs(y.y[i]), an = std::fabs(yn.y[i]);
+        const double sc = atol + rtol * (ay > an ? ay : an);
+        const double q = e / sc;
+        sum = sum + q * q;
+        finite = finite && std::isfinite(yn.y[i]) && std::isfinite(k7.y[i]);
+      }
+      const double err = finite ? std::sqrt(sum / 8.0) : INFINITY;
+      if (!(err <= 1.0)) {
+        double fac = 0.2;
+        if (std::isfinite(err)) {
+          fac = 0.9 / std::sqrt(std::sqrt(err));
+          if (fac < 0.2) fac = 0.2;
+        }
+        h = h * fac;
+        continue;
+      }
+      double fac = 5.0;
+      if (err > 0.0) {
+        fac = 0.9 / std::sqrt(std::sqrt(err));
+        if (fac > 5.0) fac = 5.0;
+        if (fac < 0.2) fac = 0.2;
+      }
+      y = yn;
+      k1 = k7;
+      h = h * fac;
+      accepted = true;
+    }
+    if (!accepted) return result(DIVERGED, n);
+  }
+  return result(DIVERGED, max_steps);
+}
+
 // ---------------------------------------------------------------------------
 // camera.rs
 // ---------------------------------------------------------------------------
@@ -995,6 +1093,26 @@ int orc_trace(int kind, const double* params, int math, const double* y0, int64_
       State s;
       std::memcpy(s.y, y0 + 8 * i, sizeof s.y);
       const TraceResult r = trace(m, s, step, max_steps);
+      if (g_singular) singular = true;
+      term[i] = r.term;
+      if (yfinal) std::memcpy(yfinal + 8 * i, r.final_state.y, sizeof r.final_state.y);
+      if (steps) steps[i] = r.steps;
+      if (resid) resid[i] = r.resid;
+    });
+    return singular ? -2 : 0;
+  });
+}
+
+int orc_trace_adaptive(int kind, const double* params, int math, const double* y0, int64_t n, double h0,
+                       int64_t max_steps, double rtol, double atol, int nthreads, int32_t* term, double* yfinal,
+                       int64_t* steps, double* resid) {
+  return with_metric(kind, params, math, [&](auto& m) {
+    std::atomic<bool> singular(false);
+    parallel_for(n, nthreads, [&](int64_t i) {
+      g_singular = false;
+      State s;
+      std::memcpy(s.y, y0 + 8 * i, sizeof s.y);
+      const TraceResult r = trace_adaptive(m, s, h0, max_steps, rtol, atol);
       if (g_singular) singular = true;
       term[i] = r.term;
       if (yfinal) std::memcpy(yfinal + 8 * i, r.final_state.y, sizeof r.final_state.y);

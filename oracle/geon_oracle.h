@@ -85,6 +85,11 @@ int orc_render(int kind, const double* params, int math, const double* observer,
                int nthreads, float* rgb_out, int32_t* pclass_out, int64_t* psteps_out,
                orc_render_stats* stats);
 
+/* The GPU's GEON_ADAPTIVE trace (Dormand-Prince 5(4), trace_adaptive.cu), restated. */
+int orc_trace_adaptive(int kind, const double* params, int math, const double* y0, int64_t n, double h0,
+                       int64_t max_steps, double rtol, double atol, int nthreads, int32_t* term, double* yfinal,
+                       int64_t* steps, double* resid);
+
 /* write_png's tonemap (render.rs:174-178): clamp, f32 powf(v, 1/2.2) from libm,
    *255, round, saturating cast to u8 (NaN -> 0). */
 void orc_tonemap_u8(const float* rgb, int64_t n, uint8_t* out);

@@ -139,6 +139,23 @@ def trace(kind, params, y0, step, max_steps, math=LIBM, nthreads=0):
     return term, yf, steps, resid
 
 
+def trace_adaptive(kind, params, y0, h0, max_steps, rtol=1e-10, atol=1e-12, math=LIBM, nthreads=0):
+    """The GPU's adaptive (Dormand-Prince 5(4)) trace, restated."""
+    y0, yp = _d(np.asarray(y0, dtype=np.float64).reshape(-1, 8))
+    n = y0.shape[0]
+    term = np.empty(n, dtype=np.int32)
+    yf = np.empty((n, 8))
+    steps = np.empty(n, dtype=np.int64)
+    resid = np.empty(n)
+    p, pp = _d(_params(params))
+    rc = lib().orc_trace_adaptive(kind, pp, math, yp, ctypes.c_int64(n), ctypes.c_double(h0),
+                                  ctypes.c_int64(max_steps), ctypes.c_double(rtol), ctypes.c_double(atol),
+                                  ctypes.c_int(nthreads), _p(term, ctypes.c_int32), _p(yf, ctypes.c_double),
+                                  _p(steps, ctypes.c_int64), _p(resid, ctypes.c_double))
+    _check(rc, "trace_adaptive")
+    return term, yf, steps, resid
+
+
 def camera_tetrad(kind, params, observer, math=LIBM):
     o, op = _d(observer)
     out = np.empty(16)

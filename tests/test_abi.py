@@ -106,3 +106,16 @@ def test_server_argument_errors_without_gpu(lib):
     assert lib.geon_server_submit(None, ctypes.byref(job), ctypes.byref(jid)) == -1
     assert lib.geon_server_poll(None, 1) == -1
     assert lib.geon_server_destroy(None) == 0
+
+
+def test_adaptive_tolerance_setter_without_gpu(lib):
+    import ctypes as C
+    r, a = C.c_double(), C.c_double()
+    lib.geon_get_adaptive_tolerance(C.byref(r), C.byref(a))
+    assert (r.value, a.value) == (1e-10, 1e-12)
+    assert lib.geon_set_adaptive_tolerance(-1.0, 1e-12) == -1
+    assert lib.geon_set_adaptive_tolerance(0.0, 0.0) == -1
+    assert lib.geon_set_adaptive_tolerance(1e-8, 1e-10) == 0
+    lib.geon_get_adaptive_tolerance(C.byref(r), C.byref(a))
+    assert (r.value, a.value) == (1e-8, 1e-10)
+    assert lib.geon_set_adaptive_tolerance(1e-10, 1e-12) == 0

@@ -139,3 +139,23 @@ def test_energy_conditions_report_format(orc):
                           encoding="utf-8"))["lines"]
     for math in (orc.LIBM, orc.GEON):
         assert energy.report(orc.energy_conditions(math)) == gold
+
+
+def test_oracle_adaptive_matches_fixed_step_physics(orc):
+    """The adaptive restatement on the validate_shadow rays: far fewer steps, the
+    same escape directions, and no class change except the fixed step's horizon
+    accidents and rays within 0.05 deg of the critical angle 14.269 deg."""
+    p = [1.0, 1.001, 1000.0]
+    alpha = np.radians(np.linspace(10.0, 20.0, 97))
+    y0 = orc.equatorial_ray(1.0, 20.0, alpha, math=orc.GEON)
+    tf, yff, sf, _ = orc.trace(1, p, y0, 0.01, 200000, math=orc.GEON)
+    ta, yfa, sa, _ = orc.trace_adaptive(1, p, y0, 0.01, 200000, math=orc.GEON)
+    assert sa.sum() * 100 < sf.sum()
+    # a fixed-step ray "escaping" from inside the photon sphere was thrown by the horizon step
+    thrown = (tf == 2) & (np.degrees(alpha) < 14.269)
+    diff = np.where(ta != tf)[0]
+    assert np.all(thrown[diff] | (np.abs(np.degrees(alpha[diff]) - 14.269) < 0.05))
+    esc = (tf == 2) & (ta == 2)
+    da = orc.asymptotic_direction(1, p, yfa[esc])
+    df = orc.asymptotic_direction(1, p, yff[esc])
+    assert np.max(np.arccos(np.clip(np.sum(da * df, axis=1), -1, 1))) < 1e-6
