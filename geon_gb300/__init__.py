@@ -13,8 +13,9 @@ from ._util import GeonError
 from .camera import Camera
 from .geodesic import (ADAPTIVE, FP64, MIXED, TraceResult, adaptive_tolerance, mom, pos, set_adaptive_tolerance,
                        trace, trace_dev)
-from .metric import (ALCUBIERRE, CAPTURED, DIVERGED, ESCAPED, MINKOWSKI, MORRIS_THORNE, SCHWARZSCHILD,
-                     Alcubierre, Metric, Minkowski, MorrisThorne, Schwarzschild, from_kind)
+from .metric import (ALCUBIERRE, CAPTURED, CARTESIAN, DIVERGED, ESCAPED, FIELD, MINKOWSKI, MORRIS_THORNE,
+                     SCHWARZSCHILD, SPHERICAL, Alcubierre, FieldMetric, Metric, Minkowski, MorrisThorne,
+                     Schwarzschild, from_kind)
 from .render import RenderConfig, RenderStats, render, render_u8, tonemap, write_png
 from .serve import Job, Server
 

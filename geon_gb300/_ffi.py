@@ -87,6 +87,8 @@ SIGNATURES = {
     "geon_render_config_default": (None, [ctypes.POINTER(GeonRenderConfig)]),
     "geon_metric_create": (ctypes.c_int, [ctypes.c_int, c_double_p, ctypes.c_int, ctypes.POINTER(c_void_p)]),
     "geon_metric_destroy": (ctypes.c_int, [c_void_p]),
+    "geon_metric_create_field": (ctypes.c_int, [ctypes.POINTER(GeonGrid), c_double_p, ctypes.c_int,
+                                                ctypes.POINTER(c_void_p)]),
     "geon_metric_kind": (ctypes.c_int, [c_void_p]),
     "geon_metric_name": (ctypes.c_char_p, [c_void_p]),
     "geon_metric_g": (ctypes.c_int, [c_void_p, c_double_p, c_size_t, c_double_p]),

@@ -18,6 +18,7 @@ using namespace geon;
 
 struct geon_metric {
   MetricDesc desc;
+  double* field = nullptr;  // device copy of a sampled metric's nodes (GEON_FIELD)
 };
 
 namespace {
@@ -157,6 +158,14 @@ cudaError_t launch_trace(const TraceLaunch& L0, int precision, int src, int sink
 }
 
 bool valid_precision(int p) { return p == GEON_FP64 || p == GEON_MIXED || p == GEON_ADAPTIVE; }
+
+// The precision is known and has a stepper for this metric.
+int check_precision(geon_metric_t m, int p) {
+  if (!valid_precision(p)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (p == GEON_MIXED && m->desc.kind == GEON_FIELD)
+    return fail(GEON_ERR_UNSUPPORTED, "the mixed-precision path has no stepper for a sampled metric");
+  return GEON_OK;
+}
 
 // Levels of the speculative bisection tree traced per round: as many as keep
 // nb * (2^L - 1) launch angles within 16384 rays (at most 16).
@@ -311,6 +320,7 @@ static int time_variants(const TraceLaunch& base, int src, int sink, int64_t n, 
 
 int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, double* rates_out, int* best_out) {
   if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind == GEON_FIELD) return fail(GEON_ERR_UNSUPPORTED, "no mixed-precision stepper for a sampled metric");
   if (n_rays < 0 || max_steps <= 0) return fail(GEON_ERR_INVALID, "bad calibration size");
   if (n_rays == 0) {
     // four rays per lane of the largest variant's grid: occupancy decides the
@@ -417,7 +427,44 @@ int geon_metric_create(int kind, const double* params, int nparams, geon_metric_
   return GEON_OK;
 }
 
+int geon_metric_create_field(const geon_grid* grid, const double* samples, int chart, geon_metric_t* out) {
+  if (!out) return fail(GEON_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!grid || !samples) return fail(GEON_ERR_INVALID, "null grid or samples");
+  if (chart != GEON_CHART_CARTESIAN && chart != GEON_CHART_SPHERICAL) return fail(GEON_ERR_INVALID, "unknown chart");
+  MetricDesc d;
+  std::memset(&d, 0, sizeof d);
+  d.kind = GEON_FIELD;
+  int64_t nodes = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (grid->n[a] < 1 || grid->n[a] > (int64_t)1 << 30) return fail(GEON_ERR_INVALID, "bad grid size");
+    if (!std::isfinite(grid->lo[a]) || !std::isfinite(grid->hi[a]) || (grid->n[a] > 1 && !(grid->hi[a] > grid->lo[a])))
+      return fail(GEON_ERR_INVALID, "bad grid extent");
+    d.f.lo[a] = grid->lo[a];
+    d.f.hi[a] = grid->hi[a];
+    d.f.n[a] = grid->n[a];
+    d.f.inv_d[a] = grid->n[a] > 1 ? (double)(grid->n[a] - 1) / (grid->hi[a] - grid->lo[a]) : 0.0;
+    nodes *= grid->n[a];
+  }
+  d.f.chart = chart;
+  geon_metric* m = new (std::nothrow) geon_metric;
+  if (!m) return fail(GEON_ERR_OOM, "out of host memory");
+  const size_t bytes = sizeof(double) * 10 * (size_t)nodes;
+  cudaError_t e = cudaMalloc(&m->field, bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(m->field, samples, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (m->field) cudaFree(m->field);
+    delete m;
+    return fail(e == cudaErrorMemoryAllocation ? GEON_ERR_OOM : GEON_ERR_CUDA, cudaGetErrorString(e));
+  }
+  d.f.c = m->field;
+  m->desc = d;
+  *out = m;
+  return GEON_OK;
+}
+
 int geon_metric_destroy(geon_metric_t m) {
+  if (m && m->field) cudaFree(m->field);
   delete m;
   return GEON_OK;
 }
@@ -425,7 +472,7 @@ int geon_metric_destroy(geon_metric_t m) {
 int geon_metric_kind(geon_metric_t m) { return m ? m->desc.kind : GEON_ERR_INVALID; }
 
 const char* geon_metric_name(geon_metric_t m) {
-  static const char* names[4] = {"minkowski", "schwarzschild", "alcubierre", "morris_thorne"};
+  static const char* names[5] = {"minkowski", "schwarzschild", "alcubierre", "morris_thorne", "field"};
   return m ? names[m->desc.kind] : "";
 }
 
@@ -462,7 +509,7 @@ int geon_trace_dev(geon_metric_t m, const double* y0, size_t n, double step, int
                    int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual,
                    void* stream) {
   if (int rc = check_metric(m)) return rc;
-  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (int rc = check_precision(m, precision)) return rc;
   if (n == 0) return GEON_OK;
   if (!y0 || !term || !final_state || !steps_taken || !null_residual)
     return fail(GEON_ERR_INVALID, "geon_trace_dev needs every device buffer");
@@ -487,7 +534,7 @@ int geon_trace_dev(geon_metric_t m, const double* y0, size_t n, double step, int
 int geon_trace(geon_metric_t m, const double* y0, size_t n, double step, int64_t max_steps, int precision,
                int32_t* term, double* final_state, int64_t* steps_taken, double* null_residual) {
   if (int rc = check_metric(m)) return rc;
-  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (int rc = check_precision(m, precision)) return rc;
   if (n == 0) return GEON_OK;
   if (!y0 || !term) return fail(GEON_ERR_INVALID, "null buffer");
   if (max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
@@ -570,7 +617,7 @@ static int render_any(geon_metric_t m, const geon_camera* cam, const geon_render
                       uint8_t* rgb8, geon_render_stats* stats, int32_t* pixel_class, int64_t* pixel_steps) {
   if (int rc = check_metric(m)) return rc;
   if (!cfg || (!rgb && !rgb8)) return fail(GEON_ERR_INVALID, "null buffer");
-  if (!valid_precision(cfg->precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (int rc = check_precision(m, cfg->precision)) return rc;
   if (cfg->max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
   cudaStream_t s = host_stream();
   const int64_t spa = cfg->samples_per_axis < 1 ? 1 : cfg->samples_per_axis;

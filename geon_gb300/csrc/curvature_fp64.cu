@@ -262,6 +262,7 @@ static cudaError_t launch_curv(const MetricDesc& M, int what, const double* x, i
     case KIND_SCHWARZSCHILD: return launch_curv_k<KIND_SCHWARZSCHILD, GRID>(M, what, x, n, k, nk, k_shared, out, flags, grid, seed, out2, kout, s);
     case KIND_ALCUBIERRE: return launch_curv_k<KIND_ALCUBIERRE, GRID>(M, what, x, n, k, nk, k_shared, out, flags, grid, seed, out2, kout, s);
     case KIND_MORRIS_THORNE: return launch_curv_k<KIND_MORRIS_THORNE, GRID>(M, what, x, n, k, nk, k_shared, out, flags, grid, seed, out2, kout, s);
+    case KIND_FIELD: return launch_curv_k<KIND_FIELD, GRID>(M, what, x, n, k, nk, k_shared, out, flags, grid, seed, out2, kout, s);
   }
   return cudaErrorInvalidValue;
 }

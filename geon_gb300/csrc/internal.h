@@ -10,7 +10,19 @@
 namespace geon {
 
 enum : int { TERM_NONE = -1, TERM_DIVERGED = 0, TERM_CAPTURED = 1, TERM_ESCAPED = 2 };
-enum : int { KIND_MINKOWSKI = 0, KIND_SCHWARZSCHILD = 1, KIND_ALCUBIERRE = 2, KIND_MORRIS_THORNE = 3 };
+enum : int { KIND_MINKOWSKI = 0, KIND_SCHWARZSCHILD = 1, KIND_ALCUBIERRE = 2, KIND_MORRIS_THORNE = 3,
+             KIND_FIELD = 4 };
+
+// A sampled (tensor-field) metric: the 10 unique components of g at the nodes
+// of a regular grid over the three spatial chart coordinates, used as the
+// control points of a uniform cubic B-spline (geon_metric_create_field).
+struct FieldDesc {
+  const double* c;   // device: node (i, j, k) at 10 * (i + n0 * (j + n1 * k))
+  double lo[3], hi[3];
+  double inv_d[3];   // (n - 1) / (hi - lo), 0 for an axis with one node
+  int64_t n[3];
+  int chart;         // GEON_CHART_CARTESIAN or GEON_CHART_SPHERICAL
+};
 
 // Per-metric constants, passed by value to every kernel (kernel parameters live
 // in the constant bank, so every lane reads them through the constant cache).
@@ -20,6 +32,7 @@ struct MetricDesc {
   double capture_r;  // Schwarzschild: horizon_pad * 2.0 * mass   (schwarzschild.rs:114)
   double escape_r;   // Schwarzschild: escape_radius * mass        (schwarzschild.rs:116)
   double alc_denom;  // Alcubierre: 2.0 * tanh(R / s)               (alcubierre.rs:42)
+  FieldDesc f;       // GEON_FIELD only
 };
 
 // Camera for device-side ray generation (camera.rs:113-160 with the values that

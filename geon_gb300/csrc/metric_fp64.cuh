@@ -113,8 +113,75 @@ __device__ __forceinline__ void mt_g22_g33(const MetricDesc& M, const double x[4
 // ---------------------------------------------------------------------------
 // g(x) for each metric (dense 4x4, row-major)
 // ---------------------------------------------------------------------------
+// Sampled metric (GEON_FIELD): uniform cubic B-spline weights of the local
+// coordinate t in [0, 1) and the four node indices along one axis, clamped to
+// the grid (nodes beyond an edge repeat the edge node).
+__device__ __forceinline__ void field_axis(const FieldDesc& F, int a, double x, int64_t idx[4], double w[4]) {
+  const double u = (x - F.lo[a]) * F.inv_d[a];
+  const double fl = floor(u);
+  const double t = u - fl;
+  const double fc = fmin(fmax(fl, -2.0), (double)F.n[a] + 1.0);  // NaN -> -2: g becomes NaN through t
+  const int64_t i = (int64_t)fc;
+  const double sixth = 1.0 / 6.0;
+  const double t2 = t * t, t3 = t2 * t, s = 1.0 - t;
+  w[0] = ((s * s) * s) * sixth;
+  w[1] = ((3.0 * t3 - 6.0 * t2) + 4.0) * sixth;
+  w[2] = (((-3.0 * t3 + 3.0 * t2) + 3.0 * t) + 1.0) * sixth;
+  w[3] = t3 * sixth;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int64_t j = i - 1 + q;
+    j = j < 0 ? 0 : (j > F.n[a] - 1 ? F.n[a] - 1 : j);
+    idx[q] = j;
+  }
+}
+
+// g at x: the B-spline sum over the 4x4x4 neighbouring nodes, separable (x,
+// then y, then z), for the 10 unique components (00 01 02 03 11 12 13 22 23 33).
+__device__ __forceinline__ void field_g(const FieldDesc& F, const double x[4], double g[16]) {
+  int64_t ix[4], iy[4], iz[4];
+  double wx[4], wy[4], wz[4];
+  field_axis(F, 0, x[1], ix, wx);
+  field_axis(F, 1, x[2], iy, wy);
+  field_axis(F, 2, x[3], iz, wz);
+  double acc[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) acc[q] = 0.0;
+#pragma unroll 1
+  for (int c = 0; c < 4; ++c) {
+    double accy[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) accy[q] = 0.0;
+#pragma unroll 1
+    for (int b = 0; b < 4; ++b) {
+      double accx[10];
+#pragma unroll
+      for (int q = 0; q < 10; ++q) accx[q] = 0.0;
+      const int64_t row = F.n[0] * (iy[b] + F.n[1] * iz[c]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const double* __restrict__ s = F.c + 10 * (ix[a] + row);
+#pragma unroll
+        for (int q = 0; q < 10; ++q) accx[q] = accx[q] + wx[a] * __ldg(s + q);
+      }
+#pragma unroll
+      for (int q = 0; q < 10; ++q) accy[q] = accy[q] + wy[b] * accx[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 10; ++q) acc[q] = acc[q] + wz[c] * accy[q];
+  }
+  g[0] = acc[0]; g[1] = acc[1]; g[2] = acc[2]; g[3] = acc[3];
+  g[4] = acc[1]; g[5] = acc[4]; g[6] = acc[5]; g[7] = acc[6];
+  g[8] = acc[2]; g[9] = acc[5]; g[10] = acc[7]; g[11] = acc[8];
+  g[12] = acc[3]; g[13] = acc[6]; g[14] = acc[8]; g[15] = acc[9];
+}
+
 template <int K>
 __device__ __forceinline__ void metric_g(const MetricDesc& M, const double x[4], double g[16]) {
+  if (K == KIND_FIELD) {
+    field_g(M.f, x, g);
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < 16; ++i) g[i] = 0.0;
   if (K == KIND_MINKOWSKI) {  // minkowski.rs:11-18
@@ -195,6 +262,24 @@ __device__ __forceinline__ void metric_dg(const MetricDesc& M, const double x[4]
   if (K == KIND_MINKOWSKI) {
 #pragma unroll
     for (int i = 0; i < 64; ++i) dg[i] = 0.0;
+  } else if (K == KIND_FIELD) {
+    // The field does not depend on t: the t difference is g - g = +0 exactly
+    // (for finite g), so only the three spatial differences are evaluated.
+#pragma unroll 1
+    for (int alpha = 1; alpha < 4; ++alpha) {
+      double xp[4] = {x[0], x[1], x[2], x[3]};
+      double xm[4] = {x[0], x[1], x[2], x[3]};
+      xp[alpha] += FD_H;
+      xm[alpha] -= FD_H;
+      double gp[16], gm[16];
+      field_g(M.f, xp, gp);
+      field_g(M.f, xm, gm);
+      const double two_h = 2.0 * FD_H;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) dg[16 * alpha + i] = (gp[i] - gm[i]) / two_h;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) dg[i] = 0.0;
   } else {
     metric_dg_fd<K>(M, x, dg);
   }
@@ -268,8 +353,10 @@ __device__ __forceinline__ bool metric_christoffel(const MetricDesc& M, const do
     return true;
   } else if (K == KIND_ALCUBIERRE) {
     return christoffel_alcubierre_sparse(M, x, G);
-  } else {
+  } else if (K == KIND_MORRIS_THORNE) {
     return christoffel_morris_thorne_sparse(M, x, G);
+  } else {
+    return christoffel_generic<K>(M, x, G);
   }
 }
 
@@ -290,18 +377,26 @@ __device__ __forceinline__ int metric_terminate(const MetricDesc& M, const doubl
     const double r2 = x[1] * x[1] + x[2] * x[2] + x[3] * x[3];
     if (!isfinite(r2)) return TERM_DIVERGED;
     return r2 > 1e6 ? TERM_ESCAPED : TERM_NONE;
-  } else {
+  } else if (K == KIND_MORRIS_THORNE) {
     const double l = x[1];
     if (!isfinite(l)) return TERM_DIVERGED;
     return fabs(l) > 1000.0 ? TERM_ESCAPED : TERM_NONE;
+  } else {  // sampled metric: leaving the grid ends the ray (below the inner radius of a spherical chart: Captured)
+    if (!isfinite(x[1]) || !isfinite(x[2]) || !isfinite(x[3])) return TERM_DIVERGED;
+    const FieldDesc& F = M.f;
+    if (F.chart == GEON_CHART_SPHERICAL && F.n[0] > 1 && x[1] < F.lo[0]) return TERM_CAPTURED;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      if (F.n[a] > 1 && (x[a + 1] < F.lo[a] || x[a + 1] > F.hi[a])) return TERM_ESCAPED;
+    return TERM_NONE;
   }
 }
 
 // Escape direction (mod.rs:91-108 default; alcubierre.rs:81-88; morris_thorne.rs:54-77).
 template <int K>
-__device__ __forceinline__ void metric_asymptotic_direction(const double x[4], const double p[4],
-                                                            double out[3]) {
-  if (K == KIND_ALCUBIERRE) {
+__device__ __forceinline__ void metric_asymptotic_direction(const MetricDesc& M, const double x[4],
+                                                            const double p[4], double out[3]) {
+  if (K == KIND_ALCUBIERRE || (K == KIND_FIELD && M.f.chart == GEON_CHART_CARTESIAN)) {
     const double vx = p[1], vy = p[2], vz = p[3];
     const double n = fmax(sqrt(vx * vx + vy * vy + vz * vz), 1e-30);
     out[0] = vx / n; out[1] = vy / n; out[2] = vz / n;
@@ -381,8 +476,22 @@ __device__ __forceinline__ bool geodesic_rhs(const MetricDesc& M, const double y
     return true;
   } else if (K == KIND_ALCUBIERRE) {
     return rhs_alcubierre_sparse(M, y, k);
-  } else {
+  } else if (K == KIND_MORRIS_THORNE) {
     return rhs_morris_thorne_sparse(M, y, k);
+  } else {  // the reference's dense sum (geodesic.rs:38-59)
+    double G[64];
+    const bool ok = metric_christoffel<K>(M, y, G);
+    const double p[4] = {p0, p1, p2, p3};
+#pragma unroll
+    for (int mu = 0; mu < 4; ++mu) {
+      double s = 0.0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) s += G[16 * mu + 4 * a + b] * p[a] * p[b];
+      k[4 + mu] = -s;
+    }
+    return ok;
   }
 }
 

@@ -180,6 +180,7 @@ cudaError_t launch_trace_adaptive(const TraceLaunch& L, int src, int sink, cudaS
     case KIND_SCHWARZSCHILD: return launch_k<KIND_SCHWARZSCHILD>(L, src, sink, s);
     case KIND_ALCUBIERRE: return launch_k<KIND_ALCUBIERRE>(L, src, sink, s);
     case KIND_MORRIS_THORNE: return launch_k<KIND_MORRIS_THORNE>(L, src, sink, s);
+    case KIND_FIELD: return launch_k<KIND_FIELD>(L, src, sink, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -97,7 +97,7 @@ __device__ __forceinline__ void store_ray(const TraceLaunch& L, int64_t ray, int
       rgb[0] = L.diverged_rgb[0]; rgb[1] = L.diverged_rgb[1]; rgb[2] = L.diverged_rgb[2];
     } else {
       double dir[3];
-      metric_asymptotic_direction<K>(y, y + 4, dir);
+      metric_asymptotic_direction<K>(L.M, y, y + 4, dir);
       sky_sample(dir, L.show_stars != 0, rgb);
     }
     L.srgb[3 * ray + 0] = rgb[0];

@@ -160,6 +160,7 @@ cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStrea
     case KIND_SCHWARZSCHILD: return launch_k<KIND_SCHWARZSCHILD>(L, src, sink, s);
     case KIND_ALCUBIERRE: return launch_k<KIND_ALCUBIERRE>(L, src, sink, s);
     case KIND_MORRIS_THORNE: return launch_k<KIND_MORRIS_THORNE>(L, src, sink, s);
+    case KIND_FIELD: return launch_k<KIND_FIELD>(L, src, sink, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -296,7 +297,7 @@ __global__ void pointwise_kernel(const MetricDesc M, int what, const double* __r
   if (what == PW_ASYM) {
     const double* s = in + 8 * i;
     double x[4] = {s[0], s[1], s[2], s[3]}, p[4] = {s[4], s[5], s[6], s[7]}, d[3];
-    metric_asymptotic_direction<K>(x, p, d);
+    metric_asymptotic_direction<K>(M, x, p, d);
     out[3 * i] = d[0]; out[3 * i + 1] = d[1]; out[3 * i + 2] = d[2];
     return;
   }
@@ -332,6 +333,7 @@ cudaError_t launch_pointwise(const MetricDesc& M, int what, const double* in, in
     case KIND_SCHWARZSCHILD: pointwise_kernel<KIND_SCHWARZSCHILD><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
     case KIND_ALCUBIERRE: pointwise_kernel<KIND_ALCUBIERRE><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
     case KIND_MORRIS_THORNE: pointwise_kernel<KIND_MORRIS_THORNE><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
+    case KIND_FIELD: pointwise_kernel<KIND_FIELD><<<grid, block, 0, s>>>(M, what, in, n, out, iout, flags); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -387,6 +389,7 @@ cudaError_t launch_tetrad(const MetricDesc& M, const double* obs, double* out16,
     case KIND_SCHWARZSCHILD: tetrad_kernel<KIND_SCHWARZSCHILD><<<1, 32, 0, s>>>(M, obs, out16, status); break;
     case KIND_ALCUBIERRE: tetrad_kernel<KIND_ALCUBIERRE><<<1, 32, 0, s>>>(M, obs, out16, status); break;
     case KIND_MORRIS_THORNE: tetrad_kernel<KIND_MORRIS_THORNE><<<1, 32, 0, s>>>(M, obs, out16, status); break;
+    case KIND_FIELD: tetrad_kernel<KIND_FIELD><<<1, 32, 0, s>>>(M, obs, out16, status); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

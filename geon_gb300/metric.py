@@ -11,7 +11,8 @@ import numpy as np
 from . import _ffi
 from ._util import check, dp, f64, i32p, points
 
-MINKOWSKI, SCHWARZSCHILD, ALCUBIERRE, MORRIS_THORNE = 0, 1, 2, 3
+MINKOWSKI, SCHWARZSCHILD, ALCUBIERRE, MORRIS_THORNE, FIELD = 0, 1, 2, 3, 4
+CARTESIAN, SPHERICAL = 0, 1
 DIVERGED, CAPTURED, ESCAPED = 0, 1, 2
 TERMINATION = {DIVERGED: "Diverged", CAPTURED: "Captured", ESCAPED: "Escaped", -1: None}
 
@@ -121,6 +122,49 @@ class MorrisThorne(Metric):
     def __init__(self, throat_radius=1.0):
         super().__init__((throat_radius,))
         self.throat_radius = self.params[0]
+
+
+class FieldMetric(Metric):
+    """A sampled (tensor-field) metric, geon_metric_create_field: the 10 unique
+    components of a static g at the nodes of a regular grid over (x1, x2, x3),
+    the control points of a uniform cubic B-spline (C2, so its curvature is
+    meaningful). samples: (n0*n1*n2, 10) or (n2, n1, n0, 10), x fastest, in the
+    order g00 g01 g02 g03 g11 g12 g13 g22 g23 g33. chart: CARTESIAN or SPHERICAL
+    (how escape directions read the coordinates)."""
+    kind = FIELD
+    COMPONENTS = ((0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, 2), (1, 3), (2, 2), (2, 3), (3, 3))
+
+    def __init__(self, lo, hi, n, samples, chart=CARTESIAN):
+        lib = _ffi.load()
+        grid = _ffi.GeonGrid()
+        for a in range(3):
+            grid.lo[a] = float(lo[a])
+            grid.hi[a] = float(hi[a])
+            grid.n[a] = int(n[a])
+        nodes = int(n[0]) * int(n[1]) * int(n[2])
+        s = f64(np.asarray(samples, dtype=np.float64).reshape(nodes, 10))
+        h = ctypes.c_void_p()
+        check(lib.geon_metric_create_field(grid, dp(s), int(chart), ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+        self.params = ()
+        self.lo, self.hi, self.n, self.chart = tuple(lo), tuple(hi), tuple(int(v) for v in n), int(chart)
+        self.samples = s
+
+    @staticmethod
+    def nodes(lo, hi, n, t=0.0):
+        """The node positions (n0*n1*n2, 4), x fastest."""
+        axes = [np.linspace(float(lo[a]), float(hi[a]), int(n[a])) if int(n[a]) > 1 else np.array([float(lo[a])])
+                for a in range(3)]
+        z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+        return np.stack([np.full(x.size, float(t)), x.ravel(), y.ravel(), z.ravel()], axis=1)
+
+    @classmethod
+    def sample(cls, metric, lo, hi, n, chart=CARTESIAN, t=0.0):
+        """Sample another metric's g at the grid nodes (on the GPU)."""
+        g = metric.g(cls.nodes(lo, hi, n, t)).reshape(-1, 4, 4)
+        comps = np.stack([g[:, i, j] for i, j in cls.COMPONENTS], axis=1)
+        return cls(lo, hi, n, comps, chart)
 
 
 def from_kind(kind, params=()):

@@ -56,8 +56,11 @@ enum geon_metric_kind {
   GEON_MINKOWSKI = 0,     /* metric/minkowski.rs */
   GEON_SCHWARZSCHILD = 1, /* metric/schwarzschild.rs */
   GEON_ALCUBIERRE = 2,    /* metric/alcubierre.rs */
-  GEON_MORRIS_THORNE = 3  /* metric/morris_thorne.rs */
+  GEON_MORRIS_THORNE = 3, /* metric/morris_thorne.rs */
+  GEON_FIELD = 4          /* a sampled metric (geon_metric_create_field); an extension */
 };
+/* chart of a sampled metric: how asymptotic_direction reads (x1, x2, x3) */
+enum geon_chart { GEON_CHART_CARTESIAN = 0, GEON_CHART_SPHERICAL = 1 };
 enum geon_termination { GEON_DIVERGED = 0, GEON_CAPTURED = 1, GEON_ESCAPED = 2 };
 /* GEON_ADAPTIVE (an extension; the reference lists it as a TODO at
  * integrator.rs:5-7): FP64 Dormand-Prince 5(4) with error control instead of
@@ -100,6 +103,15 @@ typedef struct {
   int64_t total_steps; /* sum of steps_taken over every traced sample */
 } geon_render_stats;
 
+/* A regular grid over the three spatial chart coordinates: n[a] points from
+ * lo[a] to hi[a] inclusive (x fastest), at time t. */
+typedef struct {
+  double lo[3];
+  double hi[3];
+  int64_t n[3];
+  double t;
+} geon_grid;
+
 const char* geon_version(void);
 /* Message of the last failed call on this thread. */
 const char* geon_last_error(void);
@@ -114,6 +126,20 @@ void geon_render_config_default(geon_render_config* cfg);
  *   MORRIS_THORNE  {throat_radius}
  * Missing trailing params take the reference's defaults. */
 int geon_metric_create(int kind, const double* params, int nparams, geon_metric_t* out);
+/* A sampled (tensor-field) metric: the phase-4 idea of g from a sampled or
+ * neural field (phase4/ARCHITECTURE.md:33-58) feeding the same finite-difference
+ * Christoffel and curvature chain as the reference's fallback metrics.
+ * samples: grid->n[0]*n[1]*n[2] nodes x 10 doubles, the unique components
+ * (g00 g01 g02 g03 g11 g12 g13 g22 g23 g33) of a static g at the nodes
+ * (x1, x2, x3) = lo + (i, j, k) * (hi - lo) / (n - 1) (grid->t ignored), node
+ * (i, j, k) at index i + n0 * (j + n1 * k). The samples are the control points of
+ * a uniform cubic B-spline, so g is C2 (its curvature is meaningful) and
+ * reproduces affine fields exactly (smoother fields to O(spacing^2)); an axis
+ * with one node is constant. Trace termination: leaving the grid box escapes
+ * (on a spherical chart, falling below the inner radius is a capture); a
+ * non-finite position diverges. The samples are copied to the device; FP64 and
+ * adaptive paths (the mixed path answers GEON_ERR_UNSUPPORTED). */
+int geon_metric_create_field(const geon_grid* grid, const double* samples, int chart, geon_metric_t* out);
 int geon_metric_destroy(geon_metric_t m);
 int geon_metric_kind(geon_metric_t m);
 /* Metric::name (metric/mod.rs:84) */
@@ -221,12 +247,6 @@ int geon_nec_contraction(geon_metric_t m, const double* x, size_t n, const doubl
  * Gram-Schmidt tetrad, n uniform on the sphere drawn from the counter-based
  * stream splitmix64(seed ^ (p*nk + q)); k_out (n*nk*4, may be NULL) returns
  * the vectors used. */
-typedef struct {
-  double lo[3];
-  double hi[3];
-  int64_t n[3];
-  double t;
-} geon_grid;
 int geon_curvature_grid(geon_metric_t m, const geon_grid* grid, size_t nk, uint64_t seed, double* einstein,
                         double* nec, double* k_out);
 int geon_curvature_grid_dev(geon_metric_t m, const geon_grid* grid, size_t nk, uint64_t seed,

@@ -823,9 +823,95 @@ void parallel_for(int64_t n, int nthreads, const std::function<void(int64_t)>& f
   for (auto& th : pool) th.join();
 }
 
+// A sampled metric (the GPU's GEON_FIELD, geon_metric_create_field): the 10
+// unique components of a static g at the nodes of a regular grid, used as the
+// control points of a uniform cubic B-spline; everything else (g^-1, dg,
+// Christoffel, curvature, trace) is the reference's generic fallback path
+// (mod.rs:25-69). The field is registered once with orc_field_set.
+struct FieldData {
+  std::vector<double> c;
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, inv_d[3] = {0, 0, 0};
+  int64_t n[3] = {1, 1, 1};
+  int chart = 0;  // 0 Cartesian, 1 spherical
+};
+FieldData g_field;
+
+template <class M>
+struct FieldMetric : MetricBase<FieldMetric<M>> {
+  const FieldData* F = &g_field;
+  void axis(int a, double x, int64_t idx[4], double w[4]) const {
+    const double u = (x - F->lo[a]) * F->inv_d[a];
+    const double fl = std::floor(u);
+    const double t = u - fl;
+    const double fc = std::fmin(std::fmax(fl, -2.0), (double)F->n[a] + 1.0);
+    const int64_t i = (int64_t)fc;
+    const double sixth = 1.0 / 6.0;
+    const double t2 = t * t, t3 = t2 * t, s = 1.0 - t;
+    w[0] = ((s * s) * s) * sixth;
+    w[1] = ((3.0 * t3 - 6.0 * t2) + 4.0) * sixth;
+    w[2] = (((-3.0 * t3 + 3.0 * t2) + 3.0 * t) + 1.0) * sixth;
+    w[3] = t3 * sixth;
+    for (int q = 0; q < 4; ++q) {
+      int64_t j = i - 1 + q;
+      idx[q] = j < 0 ? 0 : (j > F->n[a] - 1 ? F->n[a] - 1 : j);
+    }
+  }
+  Mat4 g(const Vec4& x) const {
+    int64_t ix[4], iy[4], iz[4];
+    double wx[4], wy[4], wz[4];
+    axis(0, x[1], ix, wx);
+    axis(1, x[2], iy, wy);
+    axis(2, x[3], iz, wz);
+    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < 4; ++c) {
+      double accy[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int b = 0; b < 4; ++b) {
+        double accx[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const int64_t row = F->n[0] * (iy[b] + F->n[1] * iz[c]);
+        for (int a = 0; a < 4; ++a) {
+          const double* s = F->c.data() + 10 * (ix[a] + row);
+          for (int q = 0; q < 10; ++q) accx[q] = accx[q] + wx[a] * s[q];
+        }
+        for (int q = 0; q < 10; ++q) accy[q] = accy[q] + wy[b] * accx[q];
+      }
+      for (int q = 0; q < 10; ++q) acc[q] = acc[q] + wz[c] * accy[q];
+    }
+    static const int comp[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+    Mat4 gm;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) gm.m[i][j] = acc[comp[i][j]];
+    return gm;
+  }
+  void dg(const Vec4& x, Mat4 out[4]) const { this->dg_default(x, out); }
+  Mat4 g_inv(const Vec4& x) const { return this->g_inv_default(x); }
+  Chr christoffel(const Vec4& x) const { return this->christoffel_default(x); }
+  int terminate(const Vec4& x) const {
+    if (!std::isfinite(x[1]) || !std::isfinite(x[2]) || !std::isfinite(x[3])) return DIVERGED;
+    if (F->chart == 1 && F->n[0] > 1 && x[1] < F->lo[0]) return CAPTURED;
+    for (int a = 0; a < 3; ++a)
+      if (F->n[a] > 1 && (x[a + 1] < F->lo[a] || x[a + 1] > F->hi[a])) return ESCAPED;
+    return NONE;
+  }
+  void asymptotic_direction(const Vec4& x, const Vec4& p, double out[3]) const {
+    if (F->chart == 1) {
+      this->template asym_spherical<M>(x, p, out);
+      return;
+    }
+    const double vx = p[1], vy = p[2], vz = p[3];
+    const double n = std::fmax(std::sqrt(vx * vx + vy * vy + vz * vz), 1e-30);
+    out[0] = vx / n; out[1] = vy / n; out[2] = vz / n;
+  }
+};
+
 // Dispatch a callable over the (metric kind, math mode) instantiation.
 template <class F>
 int with_metric(int kind, const double* p, int math, F&& f) {
+  if (kind == 4) {  // the sampled metric: sin/cos only in the spherical-chart escape direction
+    if (math == ORC_MATH_NUDGE) { FieldMetric<MathNudge> m; return f(m); }
+    if (math == ORC_MATH_GEON) { FieldMetric<MathGeon> m; return f(m); }
+    FieldMetric<MathLibm> m;
+    return f(m);
+  }
   if (math == ORC_MATH_NUDGE) {
     switch (kind) {
       case 0: { Minkowski<MathNudge> m; return f(m); }
@@ -1121,6 +1207,21 @@ int orc_trace_adaptive(int kind, const double* params, int math, const double* y
     });
     return singular ? -2 : 0;
   });
+}
+
+int orc_field_set(const double* lo3, const double* hi3, const int64_t* n3, int chart, const double* samples) {
+  int64_t nodes = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (n3[a] < 1) return -1;
+    g_field.lo[a] = lo3[a];
+    g_field.hi[a] = hi3[a];
+    g_field.n[a] = n3[a];
+    g_field.inv_d[a] = n3[a] > 1 ? (double)(n3[a] - 1) / (hi3[a] - lo3[a]) : 0.0;
+    nodes *= n3[a];
+  }
+  g_field.chart = chart;
+  g_field.c.assign(samples, samples + 10 * nodes);
+  return 0;
 }
 
 int orc_camera_tetrad(int kind, const double* params, int math, const double* observer, double* out16) {

@@ -85,6 +85,11 @@ int orc_render(int kind, const double* params, int math, const double* observer,
                int nthreads, float* rgb_out, int32_t* pclass_out, int64_t* psteps_out,
                orc_render_stats* stats);
 
+/* Register the sampled metric used for kind 4 (the GPU's GEON_FIELD): grid
+   lo/hi/n per spatial axis, chart 0 Cartesian / 1 spherical, samples n0*n1*n2 x
+   10 unique components (00 01 02 03 11 12 13 22 23 33), x fastest. */
+int orc_field_set(const double* lo3, const double* hi3, const int64_t* n3, int chart, const double* samples);
+
 /* The GPU's GEON_ADAPTIVE trace (Dormand-Prince 5(4), trace_adaptive.cu), restated. */
 int orc_trace_adaptive(int kind, const double* params, int math, const double* y0, int64_t n, double h0,
                        int64_t max_steps, double rtol, double atol, int nthreads, int32_t* term, double* yfinal,

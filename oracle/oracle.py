@@ -139,6 +139,16 @@ def trace(kind, params, y0, step, max_steps, math=LIBM, nthreads=0):
     return term, yf, steps, resid
 
 
+def field_set(lo, hi, n, samples, chart=0):
+    """Register the sampled metric used as kind 4 (the GPU's GEON_FIELD)."""
+    lo_, lp = _d(np.asarray(lo, dtype=np.float64))
+    hi_, hp = _d(np.asarray(hi, dtype=np.float64))
+    n_ = np.ascontiguousarray(np.asarray(n, dtype=np.int64))
+    s_, sp = _d(np.asarray(samples, dtype=np.float64).reshape(-1, 10))
+    rc = lib().orc_field_set(lp, hp, _p(n_, ctypes.c_int64), ctypes.c_int(chart), sp)
+    _check(rc, "field_set")
+
+
 def trace_adaptive(kind, params, y0, h0, max_steps, rtol=1e-10, atol=1e-12, math=LIBM, nthreads=0):
     """The GPU's adaptive (Dormand-Prince 5(4)) trace, restated."""
     y0, yp = _d(np.asarray(y0, dtype=np.float64).reshape(-1, 8))

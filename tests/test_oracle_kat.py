@@ -159,3 +159,43 @@ def test_oracle_adaptive_matches_fixed_step_physics(orc):
     da = orc.asymptotic_direction(1, p, yfa[esc])
     df = orc.asymptotic_direction(1, p, yff[esc])
     assert np.max(np.arccos(np.clip(np.sum(da * df, axis=1), -1, 1))) < 1e-6
+
+
+def _affine_samples(nodes):
+    # g = eta + a linear function of (x, y, z): reproduced exactly by the B-spline
+    x, y, z = nodes[:, 1], nodes[:, 2], nodes[:, 3]
+    comps = np.zeros((len(nodes), 10))
+    comps[:, 0] = -1.0 + 0.01 * x - 0.02 * z
+    comps[:, 1] = 0.03 * y
+    comps[:, 4] = 1.0 + 0.02 * y
+    comps[:, 6] = -0.01 * x
+    comps[:, 7] = 1.0 + 0.015 * z
+    comps[:, 9] = 1.0 - 0.01 * x + 0.005 * y
+    return comps
+
+
+def _grid_nodes(lo, hi, n):
+    axes = [np.linspace(lo[a], hi[a], n[a]) for a in range(3)]
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    return np.stack([np.zeros(x.size), x.ravel(), y.ravel(), z.ravel()], axis=1)
+
+
+def test_oracle_field_reproduces_affine_metric(orc):
+    """The sampled metric's B-spline reproduces an affine field exactly (up to
+    rounding) inside the grid, and a constant field gives zero curvature."""
+    lo, hi, n = (-1.0, -2.0, 0.0), (1.0, 2.0, 1.5), (9, 11, 7)
+    nodes = _grid_nodes(lo, hi, n)
+    orc.field_set(lo, hi, n, _affine_samples(nodes))
+    rng = np.random.default_rng(3)
+    x = np.stack([np.zeros(50), rng.uniform(-0.7, 0.7, 50), rng.uniform(-1.5, 1.5, 50), rng.uniform(0.3, 1.1, 50)], 1)
+    g = orc.metric_g(4, [], x, math=orc.GEON).reshape(-1, 4, 4)
+    want = _affine_samples(x)
+    idx = ((0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, 2), (1, 3), (2, 2), (2, 3), (3, 3))
+    for q, (i, j) in enumerate(idx):
+        assert np.max(np.abs(g[:, i, j] - want[:, q])) < 1e-14
+        assert np.array_equal(g[:, i, j], g[:, j, i])
+    flat = np.zeros((len(nodes), 10))
+    flat[:, 0], flat[:, 4], flat[:, 7], flat[:, 9] = -1.0, 1.0, 1.0, 1.0
+    orc.field_set(lo, hi, n, flat)
+    rs = orc.curvature(4, [], x, "ricci_scalar", math=orc.GEON)
+    assert np.max(np.abs(rs)) < 1e-5
