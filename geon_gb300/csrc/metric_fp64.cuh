@@ -114,62 +114,95 @@ __device__ __forceinline__ void mt_g22_g33(const MetricDesc& M, const double x[4
 // g(x) for each metric (dense 4x4, row-major)
 // ---------------------------------------------------------------------------
 // Sampled metric (GEON_FIELD): uniform cubic B-spline weights of the local
-// coordinate t in [0, 1) and the four node indices along one axis, clamped to
-// the grid (nodes beyond an edge repeat the edge node).
-__device__ __forceinline__ void field_axis(const FieldDesc& F, int a, double x, int64_t idx[4], double w[4]) {
-  const double u = (x - F.lo[a]) * F.inv_d[a];
+// coordinate t in [0, 1) and the first of the four node indices along one axis
+// (nodes beyond an edge repeat the edge node). Everything here is fully
+// unrolled so that no array of the evaluation lives in local memory.
+struct FieldAxis {
+  int64_t i0, i1, i2, i3;
+  double w0, w1, w2, w3;
+};
+
+__device__ __forceinline__ int64_t field_clamp(int64_t j, int64_t n) { return j < 0 ? 0 : (j > n - 1 ? n - 1 : j); }
+
+__device__ __forceinline__ FieldAxis field_axis(double lo, double inv_d, int64_t n, double x) {
+  const double u = (x - lo) * inv_d;
   const double fl = floor(u);
   const double t = u - fl;
-  const double fc = fmin(fmax(fl, -2.0), (double)F.n[a] + 1.0);  // NaN -> -2: g becomes NaN through t
+  const double fc = fmin(fmax(fl, -2.0), (double)n + 1.0);  // NaN -> -2: g becomes NaN through t
   const int64_t i = (int64_t)fc;
   const double sixth = 1.0 / 6.0;
   const double t2 = t * t, t3 = t2 * t, s = 1.0 - t;
-  w[0] = ((s * s) * s) * sixth;
-  w[1] = ((3.0 * t3 - 6.0 * t2) + 4.0) * sixth;
-  w[2] = (((-3.0 * t3 + 3.0 * t2) + 3.0 * t) + 1.0) * sixth;
-  w[3] = t3 * sixth;
+  FieldAxis A;
+  A.w0 = ((s * s) * s) * sixth;
+  A.w1 = ((3.0 * t3 - 6.0 * t2) + 4.0) * sixth;
+  A.w2 = (((-3.0 * t3 + 3.0 * t2) + 3.0 * t) + 1.0) * sixth;
+  A.w3 = t3 * sixth;
+  A.i0 = field_clamp(i - 1, n);
+  A.i1 = field_clamp(i, n);
+  A.i2 = field_clamp(i + 1, n);
+  A.i3 = field_clamp(i + 2, n);
+  return A;
+}
+
+// acc[q] = acc[q] + w * s[q] over the 10 components of one node
+__device__ __forceinline__ void field_madd(double acc[10], double w, const double* __restrict__ s) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    int64_t j = i - 1 + q;
-    j = j < 0 ? 0 : (j > F.n[a] - 1 ? F.n[a] - 1 : j);
-    idx[q] = j;
-  }
+  for (int q = 0; q < 10; ++q) acc[q] = acc[q] + w * __ldg(s + q);
+}
+
+// One row along x: the 4 nodes of (j, k), weighted by the x weights.
+__device__ __forceinline__ void field_row(const FieldDesc& F, const FieldAxis& X, int64_t j, int64_t k,
+                                          double out[10]) {
+#pragma unroll
+  for (int q = 0; q < 10; ++q) out[q] = 0.0;
+  const int64_t row = F.n[0] * (j + F.n[1] * k);
+  field_madd(out, X.w0, F.c + 10 * (X.i0 + row));
+  field_madd(out, X.w1, F.c + 10 * (X.i1 + row));
+  field_madd(out, X.w2, F.c + 10 * (X.i2 + row));
+  field_madd(out, X.w3, F.c + 10 * (X.i3 + row));
+}
+
+// One plane along y at slice k: 4 rows weighted by the y weights.
+__device__ __forceinline__ void field_plane(const FieldDesc& F, const FieldAxis& X, const FieldAxis& Y, int64_t k,
+                                            double out[10]) {
+#pragma unroll
+  for (int q = 0; q < 10; ++q) out[q] = 0.0;
+  double r[10];
+  field_row(F, X, Y.i0, k, r);
+#pragma unroll
+  for (int q = 0; q < 10; ++q) out[q] = out[q] + Y.w0 * r[q];
+  field_row(F, X, Y.i1, k, r);
+#pragma unroll
+  for (int q = 0; q < 10; ++q) out[q] = out[q] + Y.w1 * r[q];
+  field_row(F, X, Y.i2, k, r);
+#pragma unroll
+  for (int q = 0; q < 10; ++q) out[q] = out[q] + Y.w2 * r[q];
+  field_row(F, X, Y.i3, k, r);
+#pragma unroll
+  for (int q = 0; q < 10; ++q) out[q] = out[q] + Y.w3 * r[q];
 }
 
 // g at x: the B-spline sum over the 4x4x4 neighbouring nodes, separable (x,
 // then y, then z), for the 10 unique components (00 01 02 03 11 12 13 22 23 33).
 __device__ __forceinline__ void field_g(const FieldDesc& F, const double x[4], double g[16]) {
-  int64_t ix[4], iy[4], iz[4];
-  double wx[4], wy[4], wz[4];
-  field_axis(F, 0, x[1], ix, wx);
-  field_axis(F, 1, x[2], iy, wy);
-  field_axis(F, 2, x[3], iz, wz);
-  double acc[10];
+  const FieldAxis X = field_axis(F.lo[0], F.inv_d[0], F.n[0], x[1]);
+  const FieldAxis Y = field_axis(F.lo[1], F.inv_d[1], F.n[1], x[2]);
+  const FieldAxis Z = field_axis(F.lo[2], F.inv_d[2], F.n[2], x[3]);
+  double acc[10], pl[10];
 #pragma unroll
   for (int q = 0; q < 10; ++q) acc[q] = 0.0;
-#pragma unroll 1
-  for (int c = 0; c < 4; ++c) {
-    double accy[10];
+  field_plane(F, X, Y, Z.i0, pl);
 #pragma unroll
-    for (int q = 0; q < 10; ++q) accy[q] = 0.0;
-#pragma unroll 1
-    for (int b = 0; b < 4; ++b) {
-      double accx[10];
+  for (int q = 0; q < 10; ++q) acc[q] = acc[q] + Z.w0 * pl[q];
+  field_plane(F, X, Y, Z.i1, pl);
 #pragma unroll
-      for (int q = 0; q < 10; ++q) accx[q] = 0.0;
-      const int64_t row = F.n[0] * (iy[b] + F.n[1] * iz[c]);
+  for (int q = 0; q < 10; ++q) acc[q] = acc[q] + Z.w1 * pl[q];
+  field_plane(F, X, Y, Z.i2, pl);
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        const double* __restrict__ s = F.c + 10 * (ix[a] + row);
+  for (int q = 0; q < 10; ++q) acc[q] = acc[q] + Z.w2 * pl[q];
+  field_plane(F, X, Y, Z.i3, pl);
 #pragma unroll
-        for (int q = 0; q < 10; ++q) accx[q] = accx[q] + wx[a] * __ldg(s + q);
-      }
-#pragma unroll
-      for (int q = 0; q < 10; ++q) accy[q] = accy[q] + wy[b] * accx[q];
-    }
-#pragma unroll
-    for (int q = 0; q < 10; ++q) acc[q] = acc[q] + wz[c] * accy[q];
-  }
+  for (int q = 0; q < 10; ++q) acc[q] = acc[q] + Z.w3 * pl[q];
   g[0] = acc[0]; g[1] = acc[1]; g[2] = acc[2]; g[3] = acc[3];
   g[4] = acc[1]; g[5] = acc[4]; g[6] = acc[5]; g[7] = acc[6];
   g[8] = acc[2]; g[9] = acc[5]; g[10] = acc[7]; g[11] = acc[8];
@@ -265,7 +298,7 @@ __device__ __forceinline__ void metric_dg(const MetricDesc& M, const double x[4]
   } else if (K == KIND_FIELD) {
     // The field does not depend on t: the t difference is g - g = +0 exactly
     // (for finite g), so only the three spatial differences are evaluated.
-#pragma unroll 1
+#pragma unroll
     for (int alpha = 1; alpha < 4; ++alpha) {
       double xp[4] = {x[0], x[1], x[2], x[3]};
       double xm[4] = {x[0], x[1], x[2], x[3]};
