@@ -158,6 +158,9 @@ SIGNATURES = {
     "geon_server_cancel": (ctypes.c_int, [c_void_p, ctypes.c_uint64]),
     "geon_server_stats_get": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonServerStats)]),
     "geon_server_destroy": (ctypes.c_int, [c_void_p]),
+    "geon_server_set_steps_per_launch": (ctypes.c_int, [c_void_p, ctypes.c_int, ctypes.c_int]),
+    "geon_server_get_steps_per_launch": (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    "geon_server_autotune": (ctypes.c_int, [c_void_p, c_double_p, ctypes.POINTER(ctypes.c_int)]),
     "geon_energy_conditions": (ctypes.c_int, [c_double_p]),
     "geon_set_adaptive_tolerance": (ctypes.c_int, [ctypes.c_double, ctypes.c_double]),
     "geon_get_adaptive_tolerance": (None, [c_double_p, c_double_p]),

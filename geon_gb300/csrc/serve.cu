@@ -242,6 +242,8 @@ struct geon_server {
   double ray_steps = 0, grid_points = 0, t_first = -1, t_last = 0;
   int64_t epochs = 0;
   uint64_t gen = 0;  // bumped by every submission and completion
+  bool in_launch = false;  // a serving launch is on the GPU (the graph may not change)
+  std::condition_variable cv_idle;
 };
 
 namespace {
@@ -579,11 +581,15 @@ void server_loop(geon_server* S) {
     }
     // 4. one serving launch: prologue, class kernels, counter copy-back
     write_claim_order(S);
+    cudaGraphExec_t graph = S->graph;
+    S->in_launch = true;
     lk.unlock();
     note_launches(1 + SERVE_CLASSES);
-    cudaError_t e = cudaGraphLaunch(S->graph, S->s_main);
+    cudaError_t e = cudaGraphLaunch(graph, S->s_main);
     if (e == cudaSuccess) e = cudaStreamSynchronize(S->s_main);
     lk.lock();
+    S->in_launch = false;
+    S->cv_idle.notify_all();
     ++S->epochs;
     if (e != cudaSuccess) {
       fail_all(S, GEON_ERR_CUDA);
@@ -693,6 +699,18 @@ void finish_loop(geon_server* S) {
     S->cv_work.notify_all();  // arena space and a slot came free
   }
 }
+
+// Re-capture the launch graph with new per-class step budgets (lock held, no
+// launch in flight).
+int rebuild_graph(geon_server* S) {
+  if (S->graph) cudaGraphExecDestroy(S->graph);
+  S->graph = nullptr;
+  return build_graph(S);
+}
+
+// Steps-per-launch candidates of the autotuner, per precision.
+constexpr int TUNE_N = 5;
+const int TUNE_STEPS[2][TUNE_N] = {{32, 64, 128, 256, 512}, {1024, 2048, 4096, 8192, 16384}};
 
 double pct(std::vector<double> v, double p) {
   if (v.empty()) return 0.0;
@@ -908,6 +926,86 @@ int geon_server_cancel(geon_server_t S, uint64_t id) {
   } else if (J->state == ST_RUNNING && !J->stop_req) {
     J->stop_req = GEON_ERR_CANCELLED;
     S->cv_work.notify_all();
+  }
+  return GEON_OK;
+}
+
+int geon_server_set_steps_per_launch(geon_server_t S, int precision, int steps) {
+  if (!S) return set_last_error(GEON_ERR_INVALID, "null server");
+  if (precision != GEON_FP64 && precision != GEON_MIXED) return set_last_error(GEON_ERR_INVALID, "unknown precision");
+  if (steps < 1 || steps > (1 << 24)) return set_last_error(GEON_ERR_INVALID, "steps per launch out of range");
+  std::unique_lock<std::mutex> lk(S->mu);
+  if (S->fatal) return set_last_error(S->fatal, "server stopped after a CUDA error");
+  S->cv_idle.wait(lk, [S] { return !S->in_launch; });
+  for (int c = 0; c < SERVE_CLASSES; ++c)
+    if ((c & 1) == (precision == GEON_MIXED ? 1 : 0)) S->iters[c] = steps;
+  if (rebuild_graph(S) != GEON_OK) {
+    fail_all(S, GEON_ERR_CUDA);
+    return set_last_error(GEON_ERR_CUDA, "re-capturing the serving launch graph");
+  }
+  return GEON_OK;
+}
+
+int geon_server_get_steps_per_launch(geon_server_t S, int precision) {
+  if (!S || (precision != GEON_FP64 && precision != GEON_MIXED)) return GEON_ERR_INVALID;
+  std::lock_guard<std::mutex> g(S->mu);
+  return S->iters[precision == GEON_MIXED ? 1 : 0];
+}
+
+int geon_server_autotune(geon_server_t S, double* rates_out, int* best_out) {
+  if (!S) return set_last_error(GEON_ERR_INVALID, "null server");
+  double rates[2][TUNE_N] = {};
+  int best[2] = {0, 0};
+  for (int pi = 0; pi < 2; ++pi) {
+    const int precision = pi == 0 ? GEON_FP64 : GEON_MIXED;
+    // calibration: a Schwarzschild render at the reference CUDA program's settings
+    // (r_obs 30, fov 60, h 0.05, cap 20000, escape 1000M), sized so every lane of
+    // the class's grid is busy for several launches
+    geon_job q;
+    std::memset(&q, 0, sizeof q);
+    q.type = GEON_JOB_RENDER;
+    q.metric_kind = GEON_SCHWARZSCHILD;
+    q.metric_params[0] = 1.0;
+    q.metric_params[1] = 1.001;
+    q.metric_params[2] = 1000.0;
+    q.nparams = 3;
+    q.precision = precision;
+    q.camera.observer[1] = 30.0;
+    q.camera.observer[2] = 1.5707963267948966;
+    q.camera.fov_y_deg = 60.0;
+    q.camera.width = pi == 0 ? 320 : 512;
+    q.camera.height = pi == 0 ? 320 : 512;
+    q.camera.forward_sign = 1;
+    geon_render_config_default(&q.render);
+    q.render.show_stars = 0;
+    std::vector<float> rgb((size_t)q.camera.width * q.camera.height * 3);
+    geon_render_stats st;
+    q.rgb = rgb.data();
+    q.render_stats = &st;
+    double best_rate = 0.0;
+    for (int k = 0; k < TUNE_N; ++k) {
+      if (int rc = geon_server_set_steps_per_launch(S, precision, TUNE_STEPS[pi][k])) return rc;
+      uint64_t id = 0;
+      const double t0 = now_s();
+      if (int rc = geon_server_submit(S, &q, &id)) return rc;
+      if (int rc = geon_server_wait(S, id, -1.0)) return rc;
+      const double dt = now_s() - t0;
+      rates[pi][k] = dt > 0.0 ? (double)st.total_steps / dt : 0.0;
+      if (rates[pi][k] > best_rate) best_rate = rates[pi][k];
+    }
+    // the fewest steps per launch (finest admission and completion granularity)
+    // within 2 % of the best rate
+    for (int k = 0; k < TUNE_N; ++k)
+      if (rates[pi][k] >= 0.98 * best_rate) {
+        best[pi] = TUNE_STEPS[pi][k];
+        break;
+      }
+    if (int rc = geon_server_set_steps_per_launch(S, precision, best[pi])) return rc;
+  }
+  if (rates_out) std::memcpy(rates_out, rates, sizeof rates);
+  if (best_out) {
+    best_out[0] = best[0];
+    best_out[1] = best[1];
   }
   return GEON_OK;
 }

@@ -162,6 +162,24 @@ class Server:
         job.nec = _addr(out["nec"])
         return self._submit(job, JOB_CURVATURE, out)
 
+    def steps_per_launch(self, precision):
+        return self._lib.geon_server_get_steps_per_launch(self._h, PRECISION[precision])
+
+    def set_steps_per_launch(self, precision, steps):
+        check(self._lib.geon_server_set_steps_per_launch(self._h, PRECISION[precision], int(steps)))
+
+    def autotune(self):
+        """Pick steps per launch per precision (geon_server_autotune) on an idle
+        server; returns {precision: {"steps": s, "rates": {steps: ray-steps/s}}}."""
+        rates = (ctypes.c_double * 10)()
+        best = (ctypes.c_int * 2)()
+        check(self._lib.geon_server_autotune(self._h, rates, best))
+        cand = {"fp64": (32, 64, 128, 256, 512), "mixed": (1024, 2048, 4096, 8192, 16384)}
+        out = {}
+        for i, p in enumerate(("fp64", "mixed")):
+            out[p] = {"steps": int(best[i]), "rates": {c: float(rates[5 * i + k]) for k, c in enumerate(cand[p])}}
+        return out
+
     def wait_all(self, timeout=None):
         rc = self._lib.geon_server_wait_all(self._h, -1.0 if timeout is None else float(timeout))
         if rc == _ffi.GEON_ERR_TIMEOUT:

@@ -379,6 +379,20 @@ int geon_server_wait_all(geon_server_t s, double timeout_s);
  * boundary. Its status becomes GEON_ERR_CANCELLED. */
 int geon_server_cancel(geon_server_t s, uint64_t id);
 int geon_server_stats_get(geon_server_t s, geon_server_stats* out);
+/* Steps per launch of the persistent serving kernels of one precision
+ * (GEON_FP64 or GEON_MIXED): each launch runs at most this many RK4 steps per
+ * lane before the host admits arrivals and finishes jobs. Defaults 128 (FP64)
+ * and 4096 (mixed). Larger: fewer host round trips; smaller: finer admission
+ * and completion granularity. */
+int geon_server_set_steps_per_launch(geon_server_t s, int precision, int steps);
+int geon_server_get_steps_per_launch(geon_server_t s, int precision);
+/* The steps-per-launch autotuner: on an idle server, times a calibration render
+ * (Schwarzschild, r_obs 30, fov 60, h 0.05, cap 20000, escape 1000M; 320^2 FP64,
+ * 512^2 mixed) through the server at 32..512 (FP64) and 1024..16384 (mixed)
+ * steps per launch, keeps for each precision the smallest value within 2 % of
+ * the fastest, and returns ray-steps/s in rates_out[2][5] (FP64 row first) and
+ * the choices in best_out[2]. */
+int geon_server_autotune(geon_server_t s, double* rates_out, int* best_out);
 /* Stops the server after the work in flight; queued requests are cancelled. */
 int geon_server_destroy(geon_server_t s);
 

@@ -119,3 +119,9 @@ def test_adaptive_tolerance_setter_without_gpu(lib):
     lib.geon_get_adaptive_tolerance(C.byref(r), C.byref(a))
     assert (r.value, a.value) == (1e-8, 1e-10)
     assert lib.geon_set_adaptive_tolerance(1e-10, 1e-12) == 0
+
+
+def test_server_tuning_argument_errors_without_gpu(lib):
+    assert lib.geon_server_set_steps_per_launch(None, 1, 4096) == -1
+    assert lib.geon_server_get_steps_per_launch(None, 1) == -1
+    assert lib.geon_server_autotune(None, None, None) == -1

@@ -189,3 +189,21 @@ def test_many_jobs_per_class(geon):
             ac, lo, hi, st = geon.shadow.bisect(geon.Schwarzschild(1.0), R_OBS, np.radians(13.0),
                                                 np.radians(15.5), iters=20, precision=p)
             assert j.result()["alpha_c"] == ac[0] and j.result()["steps"] == st[0]
+
+
+def test_steps_per_launch_autotune(geon):
+    m = geon.Schwarzschild(1.0, 1.001, 100.0)
+    cam = geon.Camera([0.0, 30.0, np.pi / 2, 0.0], 60.0, 64, 48)
+    cfg = geon.RenderConfig(precision="mixed", show_stars=True)
+    with geon.Server(1 << 30) as srv:
+        assert srv.steps_per_launch("mixed") == 4096 and srv.steps_per_launch("fp64") == 128
+        tuned = srv.autotune()
+        for p in ("fp64", "mixed"):
+            assert tuned[p]["steps"] in tuned[p]["rates"]
+            assert all(r > 0 for r in tuned[p]["rates"].values())
+            assert srv.steps_per_launch(p) == tuned[p]["steps"]
+        srv.set_steps_per_launch("mixed", 100)  # any budget gives the same bits
+        got = srv.submit_render(m, cam, cfg).result(timeout=120)
+        with pytest.raises(geon.GeonError):
+            srv.set_steps_per_launch("mixed", 0)
+    same_render(single_render(geon, m, cam, cfg), got)
