@@ -15,7 +15,7 @@ from . import _ffi
 from ._util import check
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "autotune.json")
-VARIANTS = ("no register cap", "5 blocks/SM (<=102 regs)", "6 blocks/SM (<=85 regs)")
+VARIANTS = ("no register cap", "8 blocks/SM (<=64 regs)", "10 blocks/SM (<=51 regs)")
 
 
 def _gpu_name():

@@ -294,6 +294,8 @@ int build_graph(geon_server* S) {
 cudaError_t publish(geon_server* S, HostJob* J, const ServeJob& sj) {
   const int slot = J->slot;
   S->h_jobs[slot] = sj;
+  S->h_jobs[slot].L.band = 0.0f;  // served mixed requests use the default mixed step
+  S->h_jobs[slot].L.mixed_flags = 0;
   cudaError_t e = cudaMemcpyAsync(S->d_jobs + slot, S->h_jobs + slot, sizeof sj, cudaMemcpyHostToDevice, S->s_main);
   for (int k = 0; k < 3 && e == cudaSuccess; ++k)
     e = cudaMemsetAsync(S->d_counters + (size_t)k * SERVE_MAX_JOBS + slot, 0, sizeof(unsigned long long), S->s_main);

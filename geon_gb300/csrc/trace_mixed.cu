@@ -54,11 +54,15 @@ __device__ __forceinline__ bool ff_gt(float hi, float lo, float thi, float tlo) 
   return (hi - thi) + (lo - tlo) > 0.0f;
 }
 
-template <int K>
+// Optional parts of the mixed step, compiled in only when a caller enables
+// them: the FP64 band and the per-step null re-projection. The default kernels
+// leave both out, which keeps their register demand (and code) small.
+enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2 };
+
+template <int K, int FEAT = 0>
 struct MixedStepper {
   float hi[8], lo[8];
   AConsts<float> C;
-  AConsts<double> Cd;
   float cap_hi, cap_lo, esc_hi, esc_lo;
   float h, hh, sixth;
   unsigned nsteps = 0;  // steps this ray has taken: renormalisation follows the ray, not the lane
@@ -66,7 +70,6 @@ struct MixedStepper {
 
   __device__ __forceinline__ void setup(const TraceLaunch& L) {
     C.init(L.M);
-    Cd.init(L.M);
     cap_hi = __double2float_rn(L.M.capture_r);
     cap_lo = __double2float_rn(L.M.capture_r - (double)cap_hi);
     esc_hi = __double2float_rn(L.M.escape_r);
@@ -171,7 +174,7 @@ struct MixedStepper {
 #pragma unroll
       for (int i = 0; i < 8; ++i) renormalise(hi[i], lo[i]);
     }
-    if (L.mixed_flags & MIXED_REPROJECT) {
+    if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT)) {
       float s = 0.0f;
       if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) s = sinf(hi[2]);
       const float x[4] = {hi[0], hi[1], hi[2], hi[3]};
@@ -186,6 +189,8 @@ struct MixedStepper {
 
   // FP64 RK4 with the closed-form right-hand side (band steps).
   __device__ __forceinline__ int step_fp64(const TraceLaunch& L) {
+    AConsts<double> Cd;
+    Cd.init(L.M);
     double y[8];
     to_double(y);
     double s0 = 0.0, c0 = 1.0;
@@ -229,7 +234,7 @@ struct MixedStepper {
   }
 
   __device__ __forceinline__ int step(const TraceLaunch& L) {
-    if (K != KIND_MINKOWSKI && L.band > 0.0f && in_band<K>(L.M, hi[1], hi[2], hi[3], L.band))
+    if ((FEAT & FEAT_BAND) && K != KIND_MINKOWSKI && L.band > 0.0f && in_band<K>(L.M, hi[1], hi[2], hi[3], L.band))
       return step_fp64(L);
     return step_fp32(L);
   }
@@ -257,21 +262,22 @@ struct MixedStepper {
 };
 
 // MINB is the register cap chosen by the autotuner: __launch_bounds__(128, MINB)
-// asks the compiler to fit MINB blocks per SM (1: no cap, ~124 registers;
-// 5: <= 102; 6: <= 85), trading registers for resident warps.
-template <int K, int SRC, int SINK, int MINB>
+// asks the compiler to fit MINB blocks per SM (1: no cap, 72 registers for the
+// Schwarzschild step, 7 blocks; 8: <= 64 registers; 10: <= 51), trading
+// registers (and spills) for resident warps.
+template <int K, int SRC, int SINK, int MINB, int FEAT>
 __global__ void __launch_bounds__(TRACE_BLOCK, MINB) trace_mixed_kernel(const TraceLaunch L) {
-  trace_loop<MixedStepper<K>, K, SRC, SINK>(L);
+  trace_loop<MixedStepper<K, FEAT>, K, SRC, SINK>(L);
 }
 
-template <int K, int SRC, int SINK, int MINB>
+template <int K, int SRC, int SINK, int MINB, int FEAT>
 static cudaError_t launch_mst_v(const TraceLaunch& L, cudaStream_t s) {
   static int sms = 0, per_sm = 0;
   if (sms == 0) {
     int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_mixed_kernel<K, SRC, SINK, MINB>, TRACE_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_mixed_kernel<K, SRC, SINK, MINB, FEAT>, TRACE_BLOCK, 0);
     per_sm = occ < 1 ? 1 : occ;
   }
   // persistent grid: every resident slot, minus the blocks per SM the caller
@@ -281,25 +287,33 @@ static cudaError_t launch_mst_v(const TraceLaunch& L, cudaStream_t s) {
   const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
   int grid = (int)(need < slots ? need : slots);
   if (grid < 1) grid = 1;
-  trace_mixed_kernel<K, SRC, SINK, MINB><<<grid, TRACE_BLOCK, 0, s>>>(L);
+  trace_mixed_kernel<K, SRC, SINK, MINB, FEAT><<<grid, TRACE_BLOCK, 0, s>>>(L);
   return cudaGetLastError();
 }
 
 template <int K, int SRC, int SINK>
 static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
+  const int feat = ((K != KIND_MINKOWSKI && L.band > 0.0f) ? FEAT_BAND : 0) |
+                   ((L.mixed_flags & MIXED_REPROJECT) ? FEAT_REPROJECT : 0);
+  switch (feat) {  // the optional parts run without a register cap
+    case FEAT_BAND: return launch_mst_v<K, SRC, SINK, 1, FEAT_BAND>(L, s);
+    case FEAT_REPROJECT: return launch_mst_v<K, SRC, SINK, 1, FEAT_REPROJECT>(L, s);
+    case FEAT_BAND | FEAT_REPROJECT: return launch_mst_v<K, SRC, SINK, 1, FEAT_BAND | FEAT_REPROJECT>(L, s);
+  }
   switch (L.variant) {
-    case 1: return launch_mst_v<K, SRC, SINK, 5>(L, s);
-    case 2: return launch_mst_v<K, SRC, SINK, 6>(L, s);
-    default: return launch_mst_v<K, SRC, SINK, 1>(L, s);
+    case 1: return launch_mst_v<K, SRC, SINK, 8, 0>(L, s);
+    case 2: return launch_mst_v<K, SRC, SINK, 10, 0>(L, s);
+    default: return launch_mst_v<K, SRC, SINK, 1, 0>(L, s);
   }
 }
 
 // Serving engine kernel for the mixed-precision classes (serve_common.cuh),
-// register cap of the autotuner's variant 1 (5 blocks per SM).
+// no register cap. The server runs the default mixed step (no FP64 band, no
+// re-projection).
 template <int K>
-__global__ void __launch_bounds__(TRACE_BLOCK, 5) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
+__global__ void __launch_bounds__(TRACE_BLOCK, 1) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
                                                                      ServeClass* cl, const unsigned* epoch, int budget) {
-  serve_loop<MixedStepper<K>, K>(jobs, cnt, cl, epoch, budget);
+  serve_loop<MixedStepper<K, 0>, K>(jobs, cnt, cl, epoch, budget);
 }
 
 int serve_mixed_blocks_per_sm(int kind) {

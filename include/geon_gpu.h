@@ -217,7 +217,7 @@ void geon_get_adaptive_tolerance(double* rtol, double* atol);
 void geon_set_persistent_reserve(int blocks_per_sm);
 /* Register-cap variant of the mixed kernel per metric kind and ray source
  * (source 0: camera rays and ray arrays, 1: equatorial shadow rays): 0 = no
- * cap, 1 = fit 5 blocks of 128 threads per SM, 2 = fit 6. geon_autotune_mixed
+ * cap, 1 = fit 8 blocks of 128 threads per SM, 2 = fit 10. geon_autotune_mixed
  * times every variant on calibration jobs of this metric (n_rays rays - 0 picks
  * four per lane of the widest grid - at most max_steps each; the equatorial job only for Schwarzschild), selects the
  * fastest per source and writes ray-steps/s per (source, variant) to
@@ -318,7 +318,9 @@ int geon_shadow_bisect_dev_noalloc(geon_metric_t schwarzschild, double r_obs, co
  * a request that arrives while others run joins at the next kernel launch.
  * Each result is the one the matching single-call entry point gives
  * (geon_render_ex, geon_shadow_bisect with one bracket, geon_curvature_grid),
- * bit for bit, whatever else runs beside it. */
+ * bit for bit, whatever else runs beside it. Mixed-precision requests run the
+ * default mixed step (geon_set_mixed_band / geon_set_mixed_reproject are not
+ * applied to served requests). */
 typedef struct geon_server* geon_server_t;
 enum geon_job_type { GEON_JOB_RENDER = 0, GEON_JOB_BISECT = 1, GEON_JOB_CURVATURE = 2 };
 
