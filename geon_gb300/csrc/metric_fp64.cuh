@@ -186,7 +186,7 @@ __device__ __forceinline__ void field_plane(const FieldDesc& F, const FieldAxis&
 // then y, then z), for the 10 unique components (00 01 02 03 11 12 13 22 23 33).
 // Not inlined: the finite-difference chain calls it 6 times per Christoffel
 // evaluation, and one copy of its 640 multiply-adds per kernel is enough.
-__device__ __noinline__ void field_g(const FieldDesc& F, const double x[4], double g[16]) {
+static __device__ __noinline__ void field_g(const FieldDesc& F, const double x[4], double g[16]) {
   const FieldAxis X = field_axis(F.lo[0], F.inv_d[0], F.n[0], x[1]);
   const FieldAxis Y = field_axis(F.lo[1], F.inv_d[1], F.n[1], x[2]);
   const FieldAxis Z = field_axis(F.lo[2], F.inv_d[2], F.n[2], x[3]);
