@@ -41,7 +41,7 @@ N_SWEEP = 1 << 20
 N_BRACKETS = 64
 ITERS = 40
 SCHW = [1.0, 1.001, 1000.0]
-RESERVE = 1  # persistent sweep grid keeps one block slot per SM for the concurrent bisections
+RESERVE = 1  # default block slots per SM the persistent sweep grid leaves to the concurrent bisections
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
 B_C = 3.0 * np.sqrt(3.0)
 
@@ -157,6 +157,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-rays", type=int, default=4096)
+    ap.add_argument("--reserve", type=int, default=RESERVE,
+                    help="block slots per SM the sweep leaves free for the bisections (latency vs throughput)")
     ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy leg traces every k-th sweep ray")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 leg, accuracy, e2e and CPU legs")
     # small cases for profiling only (they change the workload; never a bench line)
@@ -215,7 +217,7 @@ def main():
         sa.wait_stream(main)
         sb.wait_stream(main)
         ea0.record(sa)
-        lib.geon_set_persistent_reserve(RESERVE)  # leave room on every SM for the bisection rounds
+        lib.geon_set_persistent_reserve(args.reserve)  # leave room on every SM for the bisection rounds
         check(lib.geon_shadow_classify_dev(h, R_OBS, s_alpha.data_ptr(), s_n, STEP, MAX_STEPS, precision,
                                            d_term.data_ptr(), d_steps.data_ptr(), sa.cuda_stream))
         lib.geon_set_persistent_reserve(0)
@@ -323,6 +325,7 @@ def main():
                                "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
                    "precision": args.precision, "rays_per_gpu": N_SWEEP, "bisections_per_gpu": N_BRACKETS,
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards",
+                   "sweep_reserve_blocks_per_sm": args.reserve,
                    "mixed_kernel_variant": None if tuned is None else tuned["variant"][1],
                    "autotune_rates": None if tuned is None else tuned.get("rates")},
         "latency": {"bisection_ms_p50": float(np.percentile(bis_ms, 50)),

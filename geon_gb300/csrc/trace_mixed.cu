@@ -311,7 +311,7 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
 // no register cap. The server runs the default mixed step (no FP64 band, no
 // re-projection).
 template <int K>
-__global__ void __launch_bounds__(TRACE_BLOCK, 1) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
+__global__ void __launch_bounds__(TRACE_BLOCK, 7) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
                                                                      ServeClass* cl, const unsigned* epoch, int budget) {
   serve_loop<MixedStepper<K, 0>, K>(jobs, cnt, cl, epoch, budget);
 }
