@@ -41,7 +41,11 @@ N_SWEEP = 1 << 20
 N_BRACKETS = 64
 ITERS = 40
 SCHW = [1.0, 1.001, 1000.0]
-RESERVE = 1  # default block slots per SM the persistent sweep grid leaves to the concurrent bisections
+# Block slots per SM the persistent sweep grid leaves to the concurrent bisection
+# rounds. The bisection is a chain of dependent rounds (latency-bound), the sweep
+# throughput-bound: with 7 resident blocks per SM, leaving 3 balances the two
+# (measured on GB300: 1 -> 5.90e10, 2 -> 5.97e10, 3 -> 6.40e10 ray-steps/s).
+RESERVE = 3
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
 B_C = 3.0 * np.sqrt(3.0)
 
