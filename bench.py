@@ -46,6 +46,7 @@ SCHW = [1.0, 1.001, 1000.0]
 # throughput-bound: with 7 resident blocks per SM, leaving 3 balances the two
 # (measured on GB300: 1 -> 5.90e10, 2 -> 5.97e10, 3 -> 6.40e10 ray-steps/s).
 RESERVE = 3
+BISECT_RAYS = 16384  # speculative width of a bisection round (geon_set_bisect_rays_per_round)
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
 B_C = 3.0 * np.sqrt(3.0)
 
@@ -161,6 +162,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-rays", type=int, default=4096)
+    ap.add_argument("--bisect-rays", type=int, default=BISECT_RAYS,
+                    help="speculative bisection width (rays per round over all brackets)")
     ap.add_argument("--reserve", type=int, default=RESERVE,
                     help="block slots per SM the sweep leaves free for the bisections (latency vs throughput)")
     ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy leg traces every k-th sweep ray")
@@ -209,6 +212,8 @@ def main():
     def check(rc):
         if rc != 0:
             raise RuntimeError(lib.geon_last_error().decode())
+
+    lib.geon_set_bisect_rays_per_round(args.bisect_rays)
 
     def one_step(precision, sweep=None):
         s_alpha, s_n = sweep if sweep is not None else (d_alpha, n_sweep)
@@ -329,7 +334,7 @@ def main():
                                "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
                    "precision": args.precision, "rays_per_gpu": N_SWEEP, "bisections_per_gpu": N_BRACKETS,
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards",
-                   "sweep_reserve_blocks_per_sm": args.reserve,
+                   "sweep_reserve_blocks_per_sm": args.reserve, "bisect_rays_per_round": args.bisect_rays,
                    "mixed_kernel_variant": None if tuned is None else tuned["variant"][1],
                    "autotune_rates": None if tuned is None else tuned.get("rates")},
         "latency": {"bisection_ms_p50": float(np.percentile(bis_ms, 50)),

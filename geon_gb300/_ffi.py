@@ -163,6 +163,8 @@ SIGNATURES = {
     "geon_server_autotune": (ctypes.c_int, [c_void_p, c_double_p, ctypes.POINTER(ctypes.c_int)]),
     "geon_energy_conditions": (ctypes.c_int, [c_double_p]),
     "geon_set_adaptive_tolerance": (ctypes.c_int, [ctypes.c_double, ctypes.c_double]),
+    "geon_set_bisect_rays_per_round": (ctypes.c_int, [ctypes.c_int64]),
+    "geon_get_bisect_rays_per_round": (ctypes.c_int64, []),
     "geon_get_adaptive_tolerance": (None, [c_double_p, c_double_p]),
     "geon_launch_count": (ctypes.c_ulonglong, []),
     "geon_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, c_double_p]),

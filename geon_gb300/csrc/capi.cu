@@ -168,13 +168,17 @@ int check_precision(geon_metric_t m, int p) {
 }
 
 // Levels of the speculative bisection tree traced per round: as many as keep
-// nb * (2^L - 1) launch angles within 16384 rays (at most 16).
-int64_t bisect_levels(size_t nb) {
-  const int64_t target_rays = 16384;
+// nb * (2^L - 1) launch angles within target_rays (at most 16).
+int64_t bisect_levels_target(size_t nb, int64_t target_rays) {
   int L = 1;
   while (L < 16 && (int64_t)nb * ((1LL << (L + 1)) - 1) <= target_rays) ++L;
   return L;
 }
+
+constexpr int64_t BISECT_RAYS_DEFAULT = 16384;
+std::atomic<int64_t> g_bisect_rays{BISECT_RAYS_DEFAULT};
+
+int64_t bisect_levels(size_t nb) { return bisect_levels_target(nb, g_bisect_rays.load()); }
 
 int copy_out(void* host, const void* dev, size_t bytes, cudaStream_t s) {
   if (host && bytes) GEON_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s));
@@ -195,7 +199,7 @@ cudaError_t launch_trace_any(const TraceLaunch& L, int precision, int src, int s
 }
 void note_launches(unsigned long long n) { counted(n); }
 int set_last_error(int code, const char* msg) { return fail(code, msg); }
-int bisect_levels_for(size_t nb) { return (int)bisect_levels(nb); }
+int bisect_levels_for(size_t nb) { return (int)bisect_levels_target(nb, BISECT_RAYS_DEFAULT); }
 int camera_desc_for(geon_metric_t m, const geon_camera* cam, int64_t spa, CameraDesc& c, cudaStream_t s) {
   return make_camera(m, cam, spa, c, s);
 }
@@ -242,6 +246,14 @@ double geon_get_mixed_band(int kind) {
 }
 
 void geon_set_mixed_reproject(int on) { g_reproject.store(on ? 1 : 0); }
+
+int geon_set_bisect_rays_per_round(int64_t rays) {
+  if (rays < 1 || rays > ((int64_t)1 << 24)) return fail(GEON_ERR_INVALID, "rays per round out of range");
+  g_bisect_rays.store(rays);
+  return GEON_OK;
+}
+
+int64_t geon_get_bisect_rays_per_round(void) { return g_bisect_rays.load(); }
 
 int geon_set_adaptive_tolerance(double rtol, double atol) {
   if (!(rtol >= 0.0) || !(atol >= 0.0) || (rtol == 0.0 && atol == 0.0) || !std::isfinite(rtol) ||

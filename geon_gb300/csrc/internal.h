@@ -140,7 +140,7 @@ TraceLaunch trace_launch_defaults(geon_metric_t m, double step, int64_t max_step
 cudaError_t launch_trace_any(const TraceLaunch& L, int precision, int src, int sink, cudaStream_t s);
 void note_launches(unsigned long long n);
 int set_last_error(int code, const char* msg);
-int bisect_levels_for(size_t nb);
+int bisect_levels_for(size_t nb);  // the default speculative width (fixed: the no-alloc scratch is sized for it)
 int camera_desc_for(geon_metric_t m, const geon_camera* cam, int64_t spa, CameraDesc& c, cudaStream_t s);
 
 // pointwise "what" codes

@@ -209,6 +209,13 @@ void geon_set_mixed_reproject(int on);
  * sqrt(mean_i((e_i / (atol + rtol * max(|y_i|, |y_new_i|)))^2)) <= 1.
  * Defaults rtol 1e-10, atol 1e-12. Calls made after this use them. */
 int geon_set_adaptive_tolerance(double rtol, double atol);
+/* Width of the speculative bisection (geon_shadow_bisect*): each round traces
+ * every midpoint the next L halvings can visit, with the largest L that keeps
+ * nb * (2^L - 1) <= rays launch angles (default 16384). A wider round takes
+ * fewer dependent rounds and more rays; results do not change. The no-alloc
+ * variant keeps the default. */
+int geon_set_bisect_rays_per_round(int64_t rays);
+int64_t geon_get_bisect_rays_per_round(void);
 void geon_get_adaptive_tolerance(double* rtol, double* atol);
 /* Trace kernels are persistent (one grid fills every SM and pulls rays from a
  * device work queue). To let another job run beside one (e.g. bisections next

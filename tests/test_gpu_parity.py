@@ -338,3 +338,22 @@ def test_trace_dev_with_device_buffers(geon, orc):
     assert np.array_equal(d_term.cpu().numpy(), term)
     assert np.array_equal(d_yf.cpu().numpy(), yf)
     assert np.array_equal(d_st.cpu().numpy(), steps)
+
+
+def test_bisection_width_does_not_change_results(geon):
+    """The speculative width (rays per round) changes how many halvings one round
+    replays, never the result: every width gives the sequential loop's bits."""
+    lib = geon._load()
+    m = geon.Schwarzschild(1.0)
+    rng = np.random.default_rng(21)
+    lo = np.radians(rng.uniform(13.0, 14.0, 8))
+    hi = np.radians(rng.uniform(14.5, 15.5, 8))
+    ref = geon.shadow.bisect(m, 20.0, lo, hi, iters=23)
+    try:
+        for width in (1, 100, 65536):
+            assert lib.geon_set_bisect_rays_per_round(width) == 0
+            got = geon.shadow.bisect(m, 20.0, lo, hi, iters=23)
+            for a, b in zip(ref, got):
+                assert np.array_equal(a, b)
+    finally:
+        lib.geon_set_bisect_rays_per_round(16384)
