@@ -19,10 +19,11 @@
 //    (g^tt = -1, g^tx = -v f, g^xx = 1 - v^2 f^2), f_i = f'(r_s) (x^i - x_s^i) / r_s,
 //    f'(r_s) = (tanh^2((r_s - R)/s) - tanh^2((r_s + R)/s)) / (2 s tanh(R/s)).
 //
-// Each RHS is evaluated at base + offset: `xb` is the ray's state at the start
-// of the step (its FP32 high words) and `d` the stage offset, which carries the
-// low words. Angles use sin/cos of the base once per step and the angle-addition
-// formula per stage, so theta keeps its compensated precision near the equator.
+// The FP32 step evaluates each stage at the high words plus the stage
+// increment (the low words are below the FP32 evaluation error), except the
+// polar angle, which keeps its low word: angles use sin/cos of the base once per
+// step and the angle-addition formula per stage, so theta keeps its compensated
+// precision near the equator (cos theta ~ 1e-8 there).
 #pragma once
 #include "internal.h"
 
@@ -93,24 +94,28 @@ __device__ __forceinline__ void angle_add(T s0, T c0, T base, T d, T* s, T* c) {
 }
 
 // k = (p, dp/dlambda) at the point xb + d.
+// k = (p, dp/dlambda) at one stage point given directly: the position x1 (r,
+// l or x), x2 and x3 (y, z: Alcubierre only), the polar angle as th_base + dth
+// (Schwarzschild, Morris-Thorne: sin/cos of th_base are s0, c0) and the
+// momentum p. Unused arguments cost nothing (the compiler drops them).
 template <int K, typename T>
-__device__ __forceinline__ void rhs_analytic(const AConsts<T>& C, const T xb[8], const T d[8], T s0, T c0,
-                                             T k[8]) {
+__device__ __forceinline__ void rhs_stage(const AConsts<T>& C, T x1, T x2, T x3, T th_base, T dth, const T p[4],
+                                          T s0, T c0, T k[8]) {
   using Mt = AMath<T>;
-  const T p0 = xb[4] + d[4], p1 = xb[5] + d[5], p2 = xb[6] + d[6], p3 = xb[7] + d[7];
+  const T p0 = p[0], p1 = p[1], p2 = p[2], p3 = p[3];
   k[0] = p0; k[1] = p1; k[2] = p2; k[3] = p3;
   if (K == KIND_MINKOWSKI) {
     k[4] = (T)0; k[5] = (T)0; k[6] = (T)0; k[7] = (T)0;
   } else if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) {
     T s, c;
-    angle_add<T>(s0, c0, xb[2], d[2], &s, &c);
+    angle_add<T>(s0, c0, th_base, dth, &s, &c);
     const T as = s < (T)0 ? -s : s;
     const T cot = as < (T)1e-8 ? (T)0 : Mt::div(c, s);
     const T p3sq = p3 * p3;
     const T th_term = s * c * p3sq;                                  // -Gamma^th_phph p^ph p^ph
     const T ang = Mt::fma(s * s, p3sq, p2 * p2);                    // (p^th)^2 + sin^2 (p^ph)^2
     if (K == KIND_SCHWARZSCHILD) {
-      const T r = xb[1] + d[1];
+      const T r = x1;
       const T ir = Mt::rcp(r);
       const T f = Mt::fma(-C.two_m, ir, (T)1);
       const T A = C.m * ir * ir;
@@ -120,7 +125,7 @@ __device__ __forceinline__ void rhs_analytic(const AConsts<T>& C, const T xb[8],
       k[6] = Mt::fma((T)(-2) * ir * p1, p2, th_term);
       k[7] = (T)(-2) * p3 * Mt::fma(ir, p1, cot * p2);
     } else {
-      const T l = xb[1] + d[1];
+      const T l = x1;
       const T r2 = Mt::fma(l, l, C.b0sq);
       const T q = Mt::div(l, r2);
       k[4] = (T)0;
@@ -129,7 +134,7 @@ __device__ __forceinline__ void rhs_analytic(const AConsts<T>& C, const T xb[8],
       k[7] = (T)(-2) * p3 * Mt::fma(q, p1, cot * p2);
     }
   } else {  // Alcubierre
-    const T X = (xb[1] + d[1]) - C.ship_x, Y = xb[2] + d[2], Z = xb[3] + d[3];
+    const T X = x1 - C.ship_x, Y = x2, Z = x3;
     const T rs = Mt::sqrt(Mt::fma(X, X, Mt::fma(Y, Y, Z * Z)));
     const T tp = Mt::tanh((rs + C.R) * C.inv_s);
     const T tm = Mt::tanh((rs - C.R) * C.inv_s);
@@ -152,6 +157,15 @@ __device__ __forceinline__ void rhs_analytic(const AConsts<T>& C, const T xb[8],
     k[6] = -Qy;
     k[7] = -Qz;
   }
+}
+
+// k at the point xb + d (xb the state at the start of the step, d the stage
+// offset, which carries the low words).
+template <int K, typename T>
+__device__ __forceinline__ void rhs_analytic(const AConsts<T>& C, const T xb[8], const T d[8], T s0, T c0,
+                                             T k[8]) {
+  const T p[4] = {xb[4] + d[4], xb[5] + d[5], xb[6] + d[6], xb[7] + d[7]};
+  rhs_stage<K, T>(C, xb[1] + d[1], xb[2] + d[2], xb[3] + d[3], xb[2], d[2], p, s0, c0, k);
 }
 
 // Null re-projection: solve g(p, p) = 0 for p^t at the point x, keeping the

@@ -126,32 +126,32 @@ struct MixedStepper {
   __device__ __forceinline__ int step_fp32(const TraceLaunch& L) {
     float s0 = 0.0f, c0 = 1.0f;
     if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) sincosf(hi[2], &s0, &c0);
-    float d[8], k[8], acc[8];
+    float k[8], acc[8], p[4];
+    // stage 1 at the state (high words; the polar angle with its low word)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) d[i] = lo[i];
-    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
+    for (int i = 0; i < 4; ++i) p[i] = hi[4 + i];
+    rhs_stage<K, float>(C, hi[1], hi[2], hi[3], hi[2], lo[2], p, s0, c0, k);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      acc[i] = k[i];
-      d[i] = __fmaf_rn(hh, k[i], lo[i]);
+    for (int i = 0; i < 8; ++i) acc[i] = k[i];
+    // stages 2-4 at y + c h k
+    float rmin = 0.0f;  // lowest stage radius (Schwarzschild horizon rule)
+#pragma unroll
+    for (int st = 0; st < 3; ++st) {
+      const float c = st < 2 ? hh : h;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) p[i] = __fmaf_rn(c, k[4 + i], hi[4 + i]);
+      const float x1 = __fmaf_rn(c, k[1], hi[1]);
+      const float x2 = __fmaf_rn(c, k[2], hi[2]);
+      const float x3 = __fmaf_rn(c, k[3], hi[3]);
+      const float dth = __fmaf_rn(c, k[2], lo[2]);
+      rmin = st == 0 ? x1 : fminf(rmin, x1);
+      rhs_stage<K, float>(C, x1, x2, x3, hi[2], dth, p, s0, c0, k);
+      if (st < 2) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i] = __fmaf_rn(2.0f, k[i], acc[i]);
+      }
     }
-    float rmin = d[1];  // lowest stage radius, as an offset from hi[1]
-    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      acc[i] = __fmaf_rn(2.0f, k[i], acc[i]);
-      d[i] = __fmaf_rn(hh, k[i], lo[i]);
-    }
-    rmin = fminf(rmin, d[1]);
-    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      acc[i] = __fmaf_rn(2.0f, k[i], acc[i]);
-      d[i] = __fmaf_rn(h, k[i], lo[i]);
-    }
-    rmin = fminf(rmin, d[1]);
-    rhs_analytic<K, float>(C, hi, d, s0, c0, k);
-    if (K == KIND_SCHWARZSCHILD && !(hi[1] + rmin > C.two_m)) return STEP_HORIZON;
+    if (K == KIND_SCHWARZSCHILD && !(rmin > C.two_m)) return STEP_HORIZON;
     bool finite = true;
     float inc[8];
 #pragma unroll
