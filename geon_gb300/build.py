@@ -1,4 +1,6 @@
-"""Build the CUDA library in-tree: geon_gb300/_lib/libgeon_gpu.so (sm_103a).
+"""Build the CUDA library in-tree: geon_gb300/_lib/libgeon_gpu.so (sm_103a),
+and the C++ ports of the reference's executables over include/geon.hpp
+(geon_gb300/_lib/bin/: validate_shadow, energy_conditions, render).
 
 Every translation unit is compiled by nvcc in parallel, then linked into one
 shared library that exports the C ABI of include/geon_gpu.h. The FP64 parity
@@ -48,7 +50,41 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
+CPP = os.path.join(HERE, "cpp")
+BIN = os.path.join(OUT, "bin")
+# C++ ports of the reference's executables (bin/validate_shadow.rs,
+# bin/energy_conditions.rs, bin/render.rs) over include/geon.hpp
+PROGRAMS = ("validate_shadow", "energy_conditions", "render")
+
+
+def build_programs(force=False):
+    """Compile the C++ executables against the library (g++, C++17)."""
+    os.makedirs(BIN, exist_ok=True)
+    deps = [LIB, os.path.join(INCLUDE, "geon.hpp"), os.path.join(CPP, "rust_fmt.hpp"), os.path.abspath(__file__)]
+    newest = max(os.path.getmtime(f) for f in deps)
+    out = []
+    for name in PROGRAMS:
+        exe = os.path.join(BIN, name)
+        src = os.path.join(CPP, name + ".cpp")
+        out.append(exe)
+        if not force and os.path.exists(exe) and os.path.getmtime(exe) >= max(newest, os.path.getmtime(src)):
+            continue
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CPP}", src, "-o", exe + ".tmp",
+               f"-L{OUT}", "-lgeon_gpu", "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed on {name}.cpp:\n{r.stdout}\n{r.stderr}")
+        os.replace(exe + ".tmp", exe)
+    return out
+
+
 def build(force=False, verbose=False):
+    lib = build_library(force, verbose)
+    build_programs(force)
+    return lib
+
+
+def build_library(force=False, verbose=False):
     os.makedirs(OUT, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
         return LIB
