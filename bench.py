@@ -189,12 +189,12 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     import geon_gb300 as geon
-    from geon_gb300 import _ffi
+    from geon_gb300 import _ffi, shard
     lib = _ffi.load()
     prec = 1 if args.precision == "mixed" else 0
     m = geon.Schwarzschild(SCHW[0], SCHW[1], args.escape_radius)
     h = m.handle
-    alpha, lo, hi = workload(0x5EED + rank)
+    alpha, lo, hi = workload(shard.rank_seed(0x5EED, rank))
     n_sweep = args.rays
     alpha = alpha[:n_sweep]
     dev = torch.device("cuda", local)
@@ -268,14 +268,7 @@ def main():
     barrier()
     launches = lib.geon_launch_count() - launches0
     clocks = sampler.stop()
-    t_total = sum(times) / 1e3
-    if dist is not None:
-        tt = torch.tensor([t_total], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
-        st = torch.tensor([total_steps], dtype=torch.float64, device=dev)
-        dist.all_reduce(st)
-        total_steps = int(st.item())
+    t_total, total_steps = shard.job_totals(dist, sum(times) / 1e3, total_steps, dev)
     value = total_steps / t_total
     sweep_steps = int(d_steps.sum().item())
     sweep_term = d_term.cpu().numpy()
