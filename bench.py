@@ -603,24 +603,47 @@ def exotic_main(args):
 
 
 def curvature_main(args):
-    """Curvature grid jobs (FP64): 128^3 Alcubierre (v 2, R 2, thickness 0.5)
+    """Curvature grid jobs (FP64): 128^3 Alcubierre (v_s 0.5, R 2, sigma 8)
     Einstein + T(k,k) for 16 null vectors per point; a 4096-point Morris-Thorne
     line; 1e5 Schwarzschild vacuum points (Ricci scalar)."""
     import geon_gb300 as geon
     from oracle import oracle as orc
     geon._load()
     threads = orc.hardware_threads()
-    alc = geon.Alcubierre(2.0, 0.5, 2.0, 0.0)
+    alc = geon.Alcubierre(2.0, 0.125, 0.5, 0.0)  # R 2, thickness 1/sigma, sigma 8, v_s 0.5
     n = args.grid
     geon.curvature.grid(alc, (-4, -4, -4), (4, 4, 4), (8, 8, 8), nk=16)
     dt, (pts, ein, nec, _) = _wall(lambda: geon.curvature.grid(alc, (-4, -4, -4), (4, 4, 4), (n, n, n), nk=16), 2)
     sub = np.arange(0, len(pts), max(1, len(pts) // 2048))
     t0 = time.perf_counter()
-    oein = orc.curvature(2, [2.0, 0.5, 2.0, 0.0], pts[sub], "einstein", math=orc.GEON, nthreads=threads)
+    oein = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.GEON, nthreads=threads)
     dt_cpu = time.perf_counter() - t0
     bit_exact = bool(np.array_equal(oein.reshape(-1, 16), ein[sub].reshape(-1, 16)))
-    oein_libm = orc.curvature(2, [2.0, 0.5, 2.0, 0.0], pts[sub], "einstein", math=orc.LIBM, nthreads=threads)
+    oein_libm = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.LIBM, nthreads=threads)
     err_libm = float(np.max(np.abs(oein_libm.reshape(-1, 16) - ein[sub].reshape(-1, 16))))
+    # Kernel-only leg: the same grid job through the device-pointer entry
+    # point, outputs resident in HBM (537 MB at 128^3, larger than L2), CUDA
+    # events on the launching stream.
+    import torch
+    st = torch.cuda.current_stream()
+    ein_d = torch.empty(len(pts) * 16, dtype=torch.float64, device="cuda")
+    nec_d = torch.empty(len(pts) * 16, dtype=torch.float64, device="cuda")
+    launch = lambda: geon.curvature.grid_dev(alc, (-4, -4, -4), (4, 4, 4), (n, n, n), ein_d, nec_d, nk=16,
+                                             stream=st.cuda_stream)
+    for _ in range(3):
+        launch()
+    reps = 5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        launch()
+    e1.record(st)
+    torch.cuda.synchronize()
+    kernel_ms = e0.elapsed_time(e1) / reps
+    dev_same = bool(np.array_equal(ein_d.cpu().numpy().reshape(-1, 16), ein.reshape(-1, 16))
+                    and np.array_equal(nec_d.cpu().numpy().reshape(-1, 16), nec.reshape(-1, 16)))
+    del ein_d, nec_d
     mt = geon.MorrisThorne(1.0)
     dt_mt, (mpts, mein, mnec, _) = _wall(lambda: geon.curvature.grid(mt, (-5, np.pi / 2, 0), (5, np.pi / 2, 0),
                                                                      (4096, 1, 1), nk=16), 3)
@@ -629,9 +652,12 @@ def curvature_main(args):
                   rng.uniform(0.0, 6.2, 100000)], axis=1)
     sch = geon.Schwarzschild(1.0)
     dt_s, rs = _wall(lambda: geon.curvature.ricci_scalar(sch, x), 3)
-    _emit(f"curvature grid {n}^3 alcubierre (v 2, R 2, thickness 0.5) einstein + 16 null T(k,k) per point",
+    _emit(f"curvature grid {n}^3 alcubierre (v_s 0.5, R 2, sigma 8) einstein + 16 null T(k,k) per point",
           len(pts) / dt, "grid-points/s", 1e3 * dt, "f64",
           {"curvature": {"alcubierre_grid": {"points": len(pts), "ms": 1e3 * dt, "points_per_s": len(pts) / dt,
+                                             "kernel_ms": kernel_ms,
+                                             "kernel_points_per_s": len(pts) / (1e-3 * kernel_ms),
+                                             "device_api_same_bits": dev_same,
                                              "bit_exact_vs_oracle_geon_sample": bit_exact,
                                              "max_abs_diff_vs_oracle_libm": err_libm},
                          "morris_thorne_line": {"points": 4096, "ms": 1e3 * dt_mt, "points_per_s": 4096 / dt_mt,

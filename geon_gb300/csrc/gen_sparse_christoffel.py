@@ -214,8 +214,12 @@ def build(name, doc, spec, depends_on, evaluator):
                     dgv[al][mu][nu] = ZERO
                 else:
                     dgv[al][mu][nu] = gen.div(d, V(expr="two_h"))
+    n_dg = len(gen.lines)
     gen.lines = body + ["  const double two_h = 2.0 * FD_H;"] + gen.lines
+    n_body = len(body)
     G = christoffel(gen, g0, dgv)
+    calc = ["  const double two_h = 2.0 * FD_H;"] + gen.lines[n_body + 1:]
+    assert len(calc) >= n_dg + 1
     nan_fill = ["  if (singular) {",
                 "    const double nan = __longlong_as_double(0x7ff8000000000000LL);",
                 "    for (int i = 0; i < 64; ++i) G[i] = nan;",
@@ -230,6 +234,29 @@ def build(name, doc, spec, depends_on, evaluator):
     out += nan_fill
     out.append("  return !singular;")
     out.append("}")
+    # The same Gamma from metric values evaluated elsewhere: gv holds, for the
+    # tags _c, _p{a}, _m{a} (a over depends_on in order), the spec's runtime
+    # names in order of first appearance. Same expressions, same bits.
+    names = []
+    for row in spec:
+        for v in row:
+            if v not in ("zero", "one", "mone") and v not in names:
+                names.append(v)
+    tags = ["_c"] + [f"_{pm}{a}" for a in depends_on for pm in ("p", "m")]
+    unpack = []
+    for ti, tag in enumerate(tags):
+        for ni, nm in enumerate(names):
+            unpack.append(f"  const double {nm}{tag} = gv[{ti * len(names) + ni}];")
+    frm = [f"// {name}: Gamma from the metric values at the {len(tags)} finite-difference points (order above)",
+           f"constexpr int {name.upper()}_VALUES = {len(names)};",
+           f"__device__ __forceinline__ bool christoffel_{name}_from(const double* gv, double G[64]) {{",
+           "  bool singular;"]
+    frm += unpack + calc
+    for i, v in enumerate(G):
+        frm.append(f"  G[{i}] = {v.c()};")
+    frm += nan_fill
+    frm.append("  return !singular;")
+    frm.append("}")
     # The RHS: same Gamma code, then the sums over the nonzero entries.
     n0 = len(gen.lines)
     rl = rhs_terms(gen, G)
@@ -242,7 +269,7 @@ def build(name, doc, spec, depends_on, evaluator):
     rhs += gen.lines[:n0] + sums
     rhs += ["  k[0] = y[4]; k[1] = y[5]; k[2] = y[6]; k[3] = y[7];"] + rl
     rhs += ["  return !singular;", "}"]
-    return "\n".join(out) + "\n\n" + "\n".join(rhs), gen
+    return "\n".join(out) + "\n\n" + "\n".join(frm) + "\n\n" + "\n".join(rhs), gen
 
 
 ALC_EVAL = """  double g00{t}, g01{t};

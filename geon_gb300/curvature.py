@@ -79,6 +79,26 @@ def grid(metric, lo, hi, n, t=0.0, nk=16, seed=0x5EED, with_einstein=True, with_
     return grid_points(lo, hi, n, t), ein, nec, kk
 
 
+def grid_dev(metric, lo, hi, n, einstein, nec, nk=16, seed=0x5EED, k_out=None, t=0.0, stream=0):
+    """Device-pointer form of grid(): einstein (N*16 doubles, or None), nec
+    (N*nk doubles) and k_out (N*nk*4 doubles, or None) are device addresses
+    (ints, or objects with data_ptr()); the launch is queued on stream and not
+    waited for."""
+    g = _ffi.GeonGrid()
+    for i in range(3):
+        g.lo[i] = float(lo[i])
+        g.hi[i] = float(hi[i])
+        g.n[i] = int(n[i])
+    g.t = float(t)
+
+    def ptr(a):
+        if a is None:
+            return None
+        return a.data_ptr() if hasattr(a, "data_ptr") else int(a)
+    check(_ffi.load().geon_curvature_grid_dev(metric.handle, g, int(nk), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                              ptr(einstein), ptr(nec), ptr(k_out), int(stream)))
+
+
 def grid_points(lo, hi, n, t=0.0):
     """The points of a grid job, in its index order (x fastest)."""
     axes = []

@@ -55,3 +55,21 @@ def test_grid_schwarzschild_vacuum(geon):
     assert np.percentile(np.abs(rs), 50) < 1e-10
     assert np.max(np.abs(rs) * w) < 1e-7
     assert np.max(np.abs(ric).max(axis=(1, 2)) * w / (1 + x[:, 1] ** 2)) < 1e-9
+
+
+@pytest.mark.parametrize("kind,params,lo,hi", [
+    (0, [], (-3.0, -3.0, -3.0), (3.0, 3.0, 3.0)),
+    (1, [1.0, 1.001, 100.0], (3.0, 0.3, -3.0), (40.0, 2.8, 3.0)),
+    (2, [2.0, 0.5, 2.0, 0.0], (-4.0, -4.0, -4.0), (4.0, 4.0, 4.0)),
+    (3, [1.0], (-5.0, 0.3, -3.0), (5.0, 2.8, 3.0)),
+], ids=["minkowski", "schwarzschild", "alcubierre_default", "morris_thorne"])
+def test_grid_matches_oracle_all_metrics(geon, orc, kind, params, lo, hi):
+    """Every metric's stencil (the slots a metric depends on, shared positions)
+    against the oracle's per-point chain, at t != 0 and a ragged last block."""
+    m = geon.from_kind(kind, params)
+    pts, ein, nec, k = geon.curvature.grid(m, lo, hi, (5, 4, 3), t=1.5, nk=3, seed=77, with_k=True)
+    assert np.array_equal(ein, orc.curvature(kind, params, pts, "einstein", math=GEON_MATH))
+    # v = 2: inside the bubble g_tt > 0, no static observer, k and T(k, k) NaN
+    assert np.array_equal(nec, orc.nec(kind, params, pts, k, math=GEON_MATH), equal_nan=True)
+    if kind == 2:
+        assert np.isnan(nec).any() and not np.isnan(nec).all()
