@@ -94,6 +94,7 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
             ray = e.ray;
             n = e.n;
             st.restore(jobs[slot].L, e.w, n);
+            st.set_source(jobs[slot].src);
           }
         }
       }
@@ -140,6 +141,7 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
           else serve_load<K, SRC_ARRAY>(J.L, ray, y0);
           st.rebind(J.L);
           st.load(J.L, y0);
+          st.set_source(J.src);
         }
       }
       need = __ballot_sync(FULL, slot < 0);

@@ -57,6 +57,7 @@ struct Fp64Stepper {
       y[i] = __longlong_as_double((long long)(((unsigned long long)w[2 * i + 1] << 32) | w[2 * i]));
   }
   __device__ __forceinline__ void rebind(const TraceLaunch&) {}
+  __device__ __forceinline__ void set_source(int) {}
 };
 
 template <int K, int SRC, int SINK>

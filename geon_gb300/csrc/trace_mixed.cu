@@ -57,7 +57,27 @@ __device__ __forceinline__ bool ff_gt(float hi, float lo, float thi, float tlo) 
 // Optional parts of the mixed step, compiled in only when a caller enables
 // them: the FP64 band and the per-step null re-projection. The default kernels
 // leave both out, which keeps their register demand (and code) small.
-enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2 };
+// FEAT_PLANAR: every ray is an equatorial Schwarzschild ray (theta = pi/2,
+// p^theta = 0, bin/validate_shadow.rs:20-35); FEAT_PLANAR_DYN: a per-ray flag
+// says so (the serving kernel, whose lanes take rays of any job).
+enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2, FEAT_PLANAR = 4, FEAT_PLANAR_DYN = 8 };
+
+// Schwarzschild right-hand side on the equatorial plane: rhs_stage at
+// sin theta = 1, cos theta = 0, p^theta = 0, where its theta terms vanish
+// (Gamma^th_phph = -sin cos, Gamma^ph_thph p^th, p^th p^th) and what remains is
+// evaluated with the same operations. The plane is invariant under the
+// geodesic equation, so a ray that starts in it stays in it.
+__device__ __forceinline__ void rhs_planar_schw(const AConsts<float>& C, float r, float p0, float p1, float p3,
+                                                float* k4, float* k5, float* k7) {
+  using Mt = AMath<float>;
+  const float ir = Mt::rcp(r);
+  const float f = Mt::fma(-C.two_m, ir, 1.0f);
+  const float A = C.m * ir * ir;
+  const float gtr = Mt::div(A, f);
+  *k4 = -2.0f * gtr * p0 * p1;
+  *k5 = Mt::fma(-A * f, p0 * p0, Mt::fma(gtr, p1 * p1, (r - C.two_m) * (p3 * p3)));
+  *k7 = -2.0f * p3 * (ir * p1);
+}
 
 template <int K, int FEAT = 0>
 struct MixedStepper {
@@ -67,6 +87,12 @@ struct MixedStepper {
   float h, hh, sixth;
   unsigned nsteps = 0;  // steps this ray has taken: renormalisation follows the ray, not the lane
   bool ready = false;
+  bool planar = (FEAT & FEAT_PLANAR) != 0;
+
+  // Serving: the source of the ray just loaded (equatorial rays step on the plane).
+  __device__ __forceinline__ void set_source(int src) {
+    if (FEAT & FEAT_PLANAR_DYN) planar = src == SRC_EQUATORIAL;
+  }
 
   __device__ __forceinline__ void setup(const TraceLaunch& L) {
     C.init(L.M);
@@ -187,6 +213,65 @@ struct MixedStepper {
     return STEP_OK;
   }
 
+  // step_fp32 for an equatorial Schwarzschild ray: the six components that
+  // move (t, r, phi and their momenta), theta and p^theta held at their loaded
+  // values (pi/2 and 0). Same stage points, horizon rule, compensated update
+  // and renormalisation as step_fp32.
+  __device__ __forceinline__ int step_fp32_planar(const TraceLaunch& L) {
+    float k1, k4, k5, k7;
+    float p0 = hi[4], p1 = hi[5], p3 = hi[7];
+    rhs_planar_schw(C, hi[1], p0, p1, p3, &k4, &k5, &k7);
+    k1 = p1;
+    float a0 = p0, a1 = p1, a3 = p3, a4 = k4, a5 = k5, a7 = k7;
+    float k0 = p0, k3 = p3;
+    float rmin = 0.0f;
+#pragma unroll
+    for (int st = 0; st < 3; ++st) {
+      const float c = st < 2 ? hh : h;
+      p0 = __fmaf_rn(c, k4, hi[4]);
+      p1 = __fmaf_rn(c, k5, hi[5]);
+      p3 = __fmaf_rn(c, k7, hi[7]);
+      const float r = __fmaf_rn(c, k1, hi[1]);
+      rmin = st == 0 ? r : fminf(rmin, r);
+      rhs_planar_schw(C, r, p0, p1, p3, &k4, &k5, &k7);
+      k0 = p0; k1 = p1; k3 = p3;
+      if (st < 2) {
+        a0 = __fmaf_rn(2.0f, k0, a0);
+        a1 = __fmaf_rn(2.0f, k1, a1);
+        a3 = __fmaf_rn(2.0f, k3, a3);
+        a4 = __fmaf_rn(2.0f, k4, a4);
+        a5 = __fmaf_rn(2.0f, k5, a5);
+        a7 = __fmaf_rn(2.0f, k7, a7);
+      }
+    }
+    if (!(rmin > C.two_m)) return STEP_HORIZON;
+    const float i0 = sixth * (a0 + k0), i1 = sixth * (a1 + k1), i3 = sixth * (a3 + k3);
+    const float i4 = sixth * (a4 + k4), i5 = sixth * (a5 + k5), i7 = sixth * (a7 + k7);
+    if (!(isfinite(i0) && isfinite(i1) && isfinite(i3) && isfinite(i4) && isfinite(i5) && isfinite(i7)))
+      return STEP_NONFINITE;
+    fast_two_sum_update(hi[0], lo[0], i0);
+    fast_two_sum_update(hi[1], lo[1], i1);
+    fast_two_sum_update(hi[3], lo[3], i3);
+    two_sum_update(hi[4], lo[4], i4);
+    two_sum_update(hi[5], lo[5], i5);
+    two_sum_update(hi[7], lo[7], i7);
+    if ((++nsteps & 7) == 0) {
+      renormalise(hi[0], lo[0]);
+      renormalise(hi[1], lo[1]);
+      renormalise(hi[3], lo[3]);
+      renormalise(hi[4], lo[4]);
+      renormalise(hi[5], lo[5]);
+      renormalise(hi[7], lo[7]);
+    }
+    if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT)) {
+      const float x[4] = {hi[0], hi[1], hi[2], hi[3]};
+      const float p[4] = {hi[4], hi[5], 0.0f, hi[7]};
+      const float pt = null_pt<K, float>(C, x, p, 1.0f, hi[4]);
+      if (isfinite(pt)) two_sum_update(hi[4], lo[4], (pt - hi[4]) - lo[4]);
+    }
+    return STEP_OK;
+  }
+
   // FP64 RK4 with the closed-form right-hand side (band steps).
   __device__ __forceinline__ int step_fp64(const TraceLaunch& L) {
     AConsts<double> Cd;
@@ -236,6 +321,8 @@ struct MixedStepper {
   __device__ __forceinline__ int step(const TraceLaunch& L) {
     if ((FEAT & FEAT_BAND) && K != KIND_MINKOWSKI && L.band > 0.0f && in_band<K>(L.M, hi[1], hi[2], hi[3], L.band))
       return step_fp64(L);
+    if (K == KIND_SCHWARZSCHILD && (FEAT & (FEAT_PLANAR | FEAT_PLANAR_DYN)) && ((FEAT & FEAT_PLANAR) || planar))
+      return step_fp32_planar(L);
     return step_fp32(L);
   }
 
@@ -267,7 +354,8 @@ struct MixedStepper {
 // registers (and spills) for resident warps.
 template <int K, int SRC, int SINK, int MINB, int FEAT>
 __global__ void __launch_bounds__(TRACE_BLOCK, MINB) trace_mixed_kernel(const TraceLaunch L) {
-  trace_loop<MixedStepper<K, FEAT>, K, SRC, SINK>(L);
+  constexpr int PL = (SRC == SRC_EQUATORIAL && K == KIND_SCHWARZSCHILD) ? FEAT_PLANAR : 0;
+  trace_loop<MixedStepper<K, FEAT | PL>, K, SRC, SINK>(L);
 }
 
 template <int K, int SRC, int SINK, int MINB, int FEAT>
@@ -313,7 +401,7 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
 template <int K>
 __global__ void __launch_bounds__(TRACE_BLOCK, 7) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
                                                                      ServeClass* cl, const unsigned* epoch, int budget) {
-  serve_loop<MixedStepper<K, 0>, K>(jobs, cnt, cl, epoch, budget);
+  serve_loop<MixedStepper<K, K == KIND_SCHWARZSCHILD ? FEAT_PLANAR_DYN : 0>, K>(jobs, cnt, cl, epoch, budget);
 }
 
 int serve_mixed_blocks_per_sm(int kind) {
