@@ -110,6 +110,10 @@ __device__ __forceinline__ void store_ray(const TraceLaunch& L, int64_t ray, int
 }
 
 constexpr int TRACE_BLOCK = 128;
+// Steps a lane takes between two refills of its warp: the ballots and the
+// queue test are paid once per TRACE_INNER steps; a lane whose ray ends inside
+// the group waits at most TRACE_INNER - 1 steps for the next ray.
+constexpr int TRACE_INNER = 4;
 enum : int { STEP_NONFINITE = 0, STEP_OK = 1, STEP_HORIZON = 2 };
 
 // geodesic.rs:62-117 for every ray of the job, persistent over a work queue.
@@ -146,30 +150,34 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
     }
     if (__ballot_sync(FULL, ray >= 0) == 0) break;
     if (ray >= 0) {
-      int t = TERM_NONE;
-      int64_t taken = n;
-      if (n >= L.max_steps) {  // loop exhausted: Diverged with steps_taken = max_steps
-        t = TERM_DIVERGED;
-        taken = L.max_steps;
-      } else {
-        t = st.terminate(L);
-        if (t == TERM_NONE) {
-          const int r = st.step(L);
-          if (r == STEP_OK) {
-            ++n;
-          } else if (r == STEP_NONFINITE) {
-            t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
-          } else {
-            t = TERM_CAPTURED;
-            taken = n + 1;
+#pragma unroll 1
+      for (int inner = 0; inner < TRACE_INNER; ++inner) {
+        int t = TERM_NONE;
+        int64_t taken = n;
+        if (n >= L.max_steps) {  // loop exhausted: Diverged with steps_taken = max_steps
+          t = TERM_DIVERGED;
+          taken = L.max_steps;
+        } else {
+          t = st.terminate(L);
+          if (t == TERM_NONE) {
+            const int r = st.step(L);
+            if (r == STEP_OK) {
+              ++n;
+            } else if (r == STEP_NONFINITE) {
+              t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
+            } else {
+              t = TERM_CAPTURED;
+              taken = n + 1;
+            }
           }
         }
-      }
-      if (t != TERM_NONE) {
-        double y[8];
-        st.to_double(y);
-        store_ray<K, SINK>(L, ray, t, y, taken);
-        ray = -1;
+        if (t != TERM_NONE) {
+          double y[8];
+          st.to_double(y);
+          store_ray<K, SINK>(L, ray, t, y, taken);
+          ray = -1;
+          break;
+        }
       }
     }
   }
