@@ -113,7 +113,7 @@ constexpr int TRACE_BLOCK = 128;
 // Steps a lane takes between two refills of its warp: the ballots and the
 // queue test are paid once per TRACE_INNER steps; a lane whose ray ends inside
 // the group waits at most TRACE_INNER - 1 steps for the next ray.
-constexpr int TRACE_INNER = 4;
+constexpr int TRACE_INNER = 16;
 enum : int { STEP_NONFINITE = 0, STEP_OK = 1, STEP_HORIZON = 2 };
 
 // geodesic.rs:62-117 for every ray of the job, persistent over a work queue.
