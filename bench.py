@@ -796,7 +796,8 @@ if __name__ == "__main__":
         ap.add_argument("--requests", type=int, default=200)
         ap.add_argument("--rate", type=float, default=200.0)
         ap.add_argument("--budget-gb", type=int, default=64)
-        ap.add_argument("--serve-precisions", default="mixed,fp64")
+        ap.add_argument("--serve-precisions", default="mixed",
+                        help="comma list; the fp64 stream of 200 requests runs for tens of minutes")
         ap.add_argument("--size", type=int, default=2048, help="exotic: image side")
         ap.add_argument("--grid", type=int, default=128, help="curvature: grid side")
         ap.add_argument("--gpus", type=int, default=1)

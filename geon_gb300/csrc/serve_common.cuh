@@ -75,7 +75,7 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
   long long ray = 0, n = 0;
   Stepper st;
   bool resume_open = in_count > 0, jobs_open = true;
-  for (int it = 0; it < budget; ++it) {
+  for (int it = 0; it < budget; it += TRACE_INNER) {  // budget counts steps; TRACE_INNER per refill
     unsigned need = __ballot_sync(FULL, slot < 0);
     if (need && resume_open) {
       const int leader = __ffs(need) - 1;
@@ -149,36 +149,40 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
     if (__ballot_sync(FULL, slot >= 0) == 0) break;
     if (slot >= 0) {
       const TraceLaunch& L = jobs[slot].L;
-      int t = TERM_NONE;
-      long long taken = n;
-      if (n >= L.max_steps) {
-        t = TERM_DIVERGED;
-        taken = L.max_steps;
-      } else {
-        t = st.terminate(L);
-        if (t == TERM_NONE) {
-          const int r = st.step(L);
-          if (r == STEP_OK) {
-            ++n;
-          } else if (r == STEP_NONFINITE) {
-            t = TERM_DIVERGED;
-          } else {
-            t = TERM_CAPTURED;
-            taken = n + 1;
+#pragma unroll 1
+      for (int inner = 0; inner < TRACE_INNER; ++inner) {
+        int t = TERM_NONE;
+        long long taken = n;
+        if (n >= L.max_steps) {
+          t = TERM_DIVERGED;
+          taken = L.max_steps;
+        } else {
+          t = st.terminate(L);
+          if (t == TERM_NONE) {
+            const int r = st.step(L);
+            if (r == STEP_OK) {
+              ++n;
+            } else if (r == STEP_NONFINITE) {
+              t = TERM_DIVERGED;
+            } else {
+              t = TERM_CAPTURED;
+              taken = n + 1;
+            }
           }
         }
-      }
-      if (t != TERM_NONE) {
-        double y[8];
-        st.to_double(y);
-        const int sink = jobs[slot].sink;
-        if (sink == SINK_RENDER) store_ray<K, SINK_RENDER>(L, ray, t, y, taken);
-        else if (sink == SINK_SHADOW) store_ray<K, SINK_SHADOW>(L, ray, t, y, taken);
-        else store_ray<K, SINK_TRACE>(L, ray, t, y, taken);
-        atomicAdd(&cnt.steps[slot], (unsigned long long)taken);
-        __threadfence();
-        atomicAdd(&cnt.done[slot], 1ull);
-        slot = -1;
+        if (t != TERM_NONE) {
+          double y[8];
+          st.to_double(y);
+          const int sink = jobs[slot].sink;
+          if (sink == SINK_RENDER) store_ray<K, SINK_RENDER>(L, ray, t, y, taken);
+          else if (sink == SINK_SHADOW) store_ray<K, SINK_SHADOW>(L, ray, t, y, taken);
+          else store_ray<K, SINK_TRACE>(L, ray, t, y, taken);
+          atomicAdd(&cnt.steps[slot], (unsigned long long)taken);
+          __threadfence();
+          atomicAdd(&cnt.done[slot], 1ull);
+          slot = -1;
+          break;
+        }
       }
     }
   }

@@ -84,6 +84,7 @@ struct MixedStepper {
   float hi[8], lo[8];
   AConsts<float> C;
   float cap_hi, cap_lo, esc_hi, esc_lo;
+  float cap_far, esc_far;  // cap_hi (1 + 2^-10), esc_hi (1 - 2^-10)
   float h, hh, sixth;
   unsigned nsteps = 0;  // steps this ray has taken: renormalisation follows the ray, not the lane
   bool ready = false;
@@ -100,6 +101,8 @@ struct MixedStepper {
     cap_lo = __double2float_rn(L.M.capture_r - (double)cap_hi);
     esc_hi = __double2float_rn(L.M.escape_r);
     esc_lo = __double2float_rn(L.M.escape_r - (double)esc_hi);
+    cap_far = cap_hi * (1.0f + 0x1p-10f);
+    esc_far = esc_hi * (1.0f - 0x1p-10f);
     h = (float)L.step;
     hh = (float)L.half_step;
     sixth = (float)L.sixth;
@@ -129,6 +132,9 @@ struct MixedStepper {
   __device__ __forceinline__ int terminate(const TraceLaunch&) const {
     if (K == KIND_SCHWARZSCHILD) {
       if (!isfinite(hi[1])) return TERM_DIVERGED;
+      // Far from both radii the high word decides: |lo| stays below 2^-20 of
+      // hi between renormalisations, far inside the 2^-10 margins.
+      if (hi[1] > cap_far && hi[1] < esc_far) return TERM_NONE;
       if (ff_gt(cap_hi, cap_lo, hi[1], lo[1])) return TERM_CAPTURED;
       if (ff_gt(hi[1], lo[1], esc_hi, esc_lo)) return TERM_ESCAPED;
       return TERM_NONE;
@@ -247,8 +253,12 @@ struct MixedStepper {
     if (!(rmin > C.two_m)) return STEP_HORIZON;
     const float i0 = sixth * (a0 + k0), i1 = sixth * (a1 + k1), i3 = sixth * (a3 + k3);
     const float i4 = sixth * (a4 + k4), i5 = sixth * (a5 + k5), i7 = sixth * (a7 + k7);
-    if (!(isfinite(i0) && isfinite(i1) && isfinite(i3) && isfinite(i4) && isfinite(i5) && isfinite(i7)))
-      return STEP_NONFINITE;
+    // NaN guard on the momenta: every stage value of p^t, p^r, p^phi enters
+    // k4, k5, k7 and so the momentum increments, so a non-finite t, r or phi
+    // increment (sums of those stage values) implies a non-finite momentum
+    // increment. Positions that nothing reads (t and phi for the shadow sink)
+    // are then left out by the compiler.
+    if (!(isfinite(i4) && isfinite(i5) && isfinite(i7))) return STEP_NONFINITE;
     fast_two_sum_update(hi[0], lo[0], i0);
     fast_two_sum_update(hi[1], lo[1], i1);
     fast_two_sum_update(hi[3], lo[3], i3);

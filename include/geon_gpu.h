@@ -390,7 +390,8 @@ int geon_server_cancel(geon_server_t s, uint64_t id);
 int geon_server_stats_get(geon_server_t s, geon_server_stats* out);
 /* Steps per launch of the persistent serving kernels of one precision
  * (GEON_FP64 or GEON_MIXED): each launch runs at most this many RK4 steps per
- * lane before the host admits arrivals and finishes jobs. Defaults 128 (FP64)
+ * lane before the host admits arrivals and finishes jobs (rounded up to a
+ * multiple of 16: a lane takes 16 steps between refills). Defaults 128 (FP64)
  * and 4096 (mixed). Larger: fewer host round trips; smaller: finer admission
  * and completion granularity. */
 int geon_server_set_steps_per_launch(geon_server_t s, int precision, int steps);
