@@ -17,7 +17,8 @@ device-timed step over every 4th sweep ray and the bisections), and the accuracy
 reported on a uniform 1/32 sample of the sweep.
 `--workload serve` runs the serving stream instead (serve_requests): a seeded
 Poisson stream of render, bisection and curvature requests through
-geon_gb300.Server, mixed then FP64, with p50/p99 latency.
+geon_gb300.Server (mixed; `--serve-precisions mixed,fp64` adds the FP64
+stream), with p50/p99 latency.
 `--impl reference` times the CPU restatement of the reference (oracle/) on
 the host cores instead.
 """
@@ -44,7 +45,7 @@ SCHW = [1.0, 1.001, 1000.0]
 # Block slots per SM the persistent sweep grid leaves to the concurrent bisection
 # rounds. The bisection is a chain of dependent rounds (latency-bound), the sweep
 # throughput-bound: with 8 resident blocks per SM (the planar equatorial step,
-# 63 registers) and 16 steps per refill, leaving 5 balances the two (measured on
+# 64 registers) and 16 steps per refill, leaving 5 balances the two (measured on
 # GB300 at 16384 rays per round: 4 -> 1.39e11, 5 -> 1.43e11 ray-steps/s; sweep /
 # bisection 463 / 362 ms at 5, 439 / 475 ms at 4).
 RESERVE = 5
@@ -623,6 +624,7 @@ def curvature_main(args):
     bit_exact = bool(np.array_equal(oein.reshape(-1, 16), ein[sub].reshape(-1, 16)))
     oein_libm = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.LIBM, nthreads=threads)
     err_libm = float(np.max(np.abs(oein_libm.reshape(-1, 16) - ein[sub].reshape(-1, 16))))
+    bit_exact_libm = bool(np.array_equal(oein_libm.reshape(-1, 16), ein[sub].reshape(-1, 16)))
     # Kernel-only leg: the same grid job through the device-pointer entry
     # point, outputs resident in HBM (537 MB at 128^3, larger than L2), CUDA
     # events on the launching stream.
@@ -661,7 +663,8 @@ def curvature_main(args):
                                              "kernel_points_per_s": len(pts) / (1e-3 * kernel_ms),
                                              "device_api_same_bits": dev_same,
                                              "bit_exact_vs_oracle_geon_sample": bit_exact,
-                                             "max_abs_diff_vs_oracle_libm": err_libm},
+                                             "max_abs_diff_vs_oracle_libm": err_libm,
+                                             "bit_exact_vs_oracle_libm_sample": bit_exact_libm},
                          "morris_thorne_line": {"points": 4096, "ms": 1e3 * dt_mt, "points_per_s": 4096 / dt_mt,
                                                 "T_tt_throat_check": "tests/test_gpu_curvature_grid.py"},
                          "schwarzschild_vacuum": {"points": 100000, "ms": 1e3 * dt_s, "points_per_s": 1e5 / dt_s,

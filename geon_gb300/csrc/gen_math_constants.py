@@ -1,8 +1,9 @@
-"""Derive the constants of the deterministic FP64 sin/cos/tanh from first principles.
+"""Derive the constants of the deterministic FP64 sin/cos from first principles.
 
-Each constant is the double nearest to pi/2 (split in three parts), 2/pi, ln 2
-(split in two parts), 1/ln 2 or (+-)1/n!. Run with mpmath available; the output
-is pasted verbatim into devmath.cuh (and the oracle's copy of the same method).
+Each constant is the double nearest to pi/2 (split in three parts), 2/pi or
+(+-)1/n!. Run with mpmath available; the output is pasted verbatim into
+devmath.cuh (and the oracle's copy of the same method). tanh and expm1 use the
+published constants of their method instead (devmath.cuh).
 """
 import mpmath as mp
 
@@ -24,11 +25,6 @@ def main():
         print(f"S{n} {rn((-1) ** ((n - 1) // 2) / mp.factorial(n)).hex()}")
     for n in range(4, 19, 2):
         print(f"C{n} {rn((-1) ** (n // 2) / mp.factorial(n)).hex()}")
-    ln2 = mp.log(2)
-    l1 = rn(ln2)
-    print(f"LN2_1 {l1.hex()}\nLN2_2 {rn(ln2 - l1).hex()}\nINV_LN2 {rn(1 / ln2).hex()}")
-    for n in range(2, 16):
-        print(f"E{n} {rn(1 / mp.factorial(n)).hex()}")
 
 
 if __name__ == "__main__":

@@ -39,11 +39,14 @@ enum { DIVERGED = 0, CAPTURED = 1, ESCAPED = 2, NONE = -1 };
 //    Elementary Functions, 1980) with a three-part constant and a TwoSum tail,
 //    then the Taylor series of sin and cos (coefficients (-1)^k/n!, rounded to
 //    double) evaluated by Horner's rule with fma.
-//  * expm1: reduction y = k*ln2 + r (Cody-Waite, two-part ln2), Taylor series of
-//    e^r - 1 to r^15, reconstruction 2^k*(em) + (2^k - 1).
-//  * tanh(a) = expm1(2a) / (expm1(2a) + 2) for 2^-28 <= a < 22, odd symmetry.
-// All constants are the double roundings of pi/2, 2/pi, ln 2 and 1/n!, derived
-// with mpmath by geon_gb300/csrc/gen_math_constants.py.
+//  * tanh and expm1: the published fdlibm method (Sun Microsystems, 1993), the
+//    one glibc's dbl-64 tanh and expm1 implement, with glibc's grouping of the
+//    expm1 polynomial and the multiply-adds its compiler fuses written as
+//    std::fma: equal to glibc 2.39's tanh bit for bit (see devmath.cuh, which
+//    holds the same steps; the two must stay identical).
+// The sin/cos constants are the double roundings of pi/2, 2/pi and 1/n!,
+// derived with mpmath by geon_gb300/csrc/gen_math_constants.py; the expm1
+// constants are the published ones.
 // ---------------------------------------------------------------------------
 constexpr double GM_PIO2_1 = 0x1.921fb54442d18p+0;
 constexpr double GM_PIO2_2 = 0x1.1a62633145c07p-54;
@@ -65,23 +68,15 @@ constexpr double GM_C12 = 0x1.1eed8eff8d898p-29;
 constexpr double GM_C14 = -0x1.93974a8c07c9dp-37;
 constexpr double GM_C16 = 0x1.ae7f3e733b81fp-45;
 constexpr double GM_C18 = -0x1.6827863b97d97p-53;
-constexpr double GM_LN2_1 = 0x1.62e42fefa39efp-1;
-constexpr double GM_LN2_2 = 0x1.abc9e3b39803fp-56;
-constexpr double GM_INV_LN2 = 0x1.71547652b82fep+0;
-constexpr double GM_E2 = 0x1.0000000000000p-1;
-constexpr double GM_E3 = 0x1.5555555555555p-3;
-constexpr double GM_E4 = 0x1.5555555555555p-5;
-constexpr double GM_E5 = 0x1.1111111111111p-7;
-constexpr double GM_E6 = 0x1.6c16c16c16c17p-10;
-constexpr double GM_E7 = 0x1.a01a01a01a01ap-13;
-constexpr double GM_E8 = 0x1.a01a01a01a01ap-16;
-constexpr double GM_E9 = 0x1.71de3a556c734p-19;
-constexpr double GM_E10 = 0x1.27e4fb7789f5cp-22;
-constexpr double GM_E11 = 0x1.ae64567f544e4p-26;
-constexpr double GM_E12 = 0x1.1eed8eff8d898p-29;
-constexpr double GM_E13 = 0x1.6124613a86d09p-33;
-constexpr double GM_E14 = 0x1.93974a8c07c9dp-37;
-constexpr double GM_E15 = 0x1.ae7f3e733b81fp-41;
+constexpr double GM_EX_LN2_HI = 0x1.62e42fee00000p-1;
+constexpr double GM_EX_LN2_LO = 0x1.a39ef35793c76p-33;
+constexpr double GM_EX_INV_LN2 = 0x1.71547652b82fep+0;
+constexpr double GM_EX_O_THRESHOLD = 0x1.62e42fefa39efp+9;
+constexpr double GM_EX_Q1 = -0x1.11111111110f4p-5;
+constexpr double GM_EX_Q2 = 0x1.a01a019fe5585p-10;
+constexpr double GM_EX_Q3 = -0x1.4ce199eaadbb7p-14;
+constexpr double GM_EX_Q4 = 0x1.0cfca86e65239p-18;
+constexpr double GM_EX_Q5 = -0x1.afdb76e09c32dp-23;
 
 void geon_sincos(double x, double* sp, double* cp) {
   if (!std::isfinite(x)) {
@@ -124,52 +119,84 @@ void geon_sincos(double x, double* sp, double* cp) {
   else { *sp = -cv; *cp = sv; }
 }
 
-double geon_expm1_pos(double y) {
-  // y in [0, 44): only the arguments tanh needs.
-  const double k = std::nearbyint(y * GM_INV_LN2);
-  const double r = std::fma(-k, GM_LN2_1, y);      // exact for |r| < 0.5
-  const double rl = -k * GM_LN2_2;                  // reduced argument is r + rl
-  double q = GM_E15;
-  q = std::fma(q, r, GM_E14);
-  q = std::fma(q, r, GM_E13);
-  q = std::fma(q, r, GM_E12);
-  q = std::fma(q, r, GM_E11);
-  q = std::fma(q, r, GM_E10);
-  q = std::fma(q, r, GM_E9);
-  q = std::fma(q, r, GM_E8);
-  q = std::fma(q, r, GM_E7);
-  q = std::fma(q, r, GM_E6);
-  q = std::fma(q, r, GM_E5);
-  q = std::fma(q, r, GM_E4);
-  q = std::fma(q, r, GM_E3);
-  q = std::fma(q, r, GM_E2);
-  const double em = r + std::fma(r * r, q, std::fma(rl, r, rl));
-  if (k == 0.0) return em;
-  const int ki = (int)k;
-  return std::ldexp(em, ki) + (std::ldexp(1.0, ki) - 1.0);
+static uint32_t gm_hi_word(double x) {
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  return (uint32_t)(b >> 32);
+}
+static double gm_from_hi_word(uint32_t hi) {
+  const uint64_t b = (uint64_t)hi << 32;
+  double x;
+  std::memcpy(&x, &b, 8);
+  return x;
 }
 
-double geon_expm1(double y) {
-  if (std::isnan(y)) return y;
-  if (y >= 0.0 && y < 44.0) return geon_expm1_pos(y);
-  // Outside what tanh needs: still deterministic, via the same kernel.
-  if (y >= 44.0) return std::exp(y) - 1.0;
-  return -geon_expm1_pos(-y) / (geon_expm1_pos(-y) + 1.0);
+// e^x - 1 for every double x; the same steps as devmath.cuh's expm1_det.
+double geon_expm1(double x) {
+  const uint32_t hxs = gm_hi_word(x);
+  const bool neg = (hxs >> 31) != 0;
+  const uint32_t hx = hxs & 0x7fffffffu;
+  if (hx >= 0x4043687Au) {                  // |x| >= 56 ln 2
+    if (hx >= 0x40862E42u) {                // |x| >= 709.78
+      if (hx >= 0x7ff00000u) return std::isnan(x) ? x + x : (neg ? -1.0 : x);
+      if (x > GM_EX_O_THRESHOLD) return INFINITY;
+    }
+    if (neg) return -1.0;
+  }
+  int k = 0;
+  double c = 0.0;
+  if (hx > 0x3fd62e42u) {                   // |x| > ln2 / 2
+    double hi, lo;
+    if (hx < 0x3FF0A2B2u) {                 // |x| < 3 ln2 / 2
+      k = neg ? -1 : 1;
+      hi = neg ? x + GM_EX_LN2_HI : x - GM_EX_LN2_HI;
+      lo = neg ? -GM_EX_LN2_LO : GM_EX_LN2_LO;
+    } else {
+      k = (int)std::fma(GM_EX_INV_LN2, x, neg ? -0.5 : 0.5);
+      const double tk = (double)k;
+      hi = std::fma(-tk, GM_EX_LN2_HI, x);
+      lo = tk * GM_EX_LN2_LO;
+    }
+    x = hi - lo;
+    c = (hi - x) - lo;
+  } else if (hx < 0x3c900000u) {            // |x| < 2^-54
+    return x;
+  }
+  const double hfx = 0.5 * x, z = x * hfx;
+  const double z2 = z * z, z4 = z2 * z2;
+  const double R = std::fma(z4, std::fma(z, GM_EX_Q5, GM_EX_Q4),
+                            std::fma(z2, std::fma(z, GM_EX_Q3, GM_EX_Q2), std::fma(z, GM_EX_Q1, 1.0)));
+  const double t = std::fma(-R, hfx, 3.0);
+  double e = z * ((R - t) / std::fma(-x, t, 6.0));
+  if (k == 0) return x - std::fma(x, e, -z);
+  e = std::fma(x, e - c, -c) - z;
+  if (k == -1) return std::fma(0.5, x - e, -0.5);
+  if (k == 1) return x < -0.25 ? -2.0 * (e - (x + 0.5)) : std::fma(2.0, x - e, 1.0);
+  const double two_k = gm_from_hi_word(0x3ff00000u + ((uint32_t)k << 20));
+  if (k <= -2 || k > 56) {
+    const double y = 1.0 - (e - x);
+    return (k == 1024 ? y * 2.0 * 0x1p1023 : y * two_k) - 1.0;
+  }
+  if (k < 20) return (gm_from_hi_word(0x3ff00000u - (0x200000u >> k)) - (e - x)) * two_k;
+  return ((x - (e + gm_from_hi_word((uint32_t)(0x3ff - k) << 20))) + 1.0) * two_k;
 }
 
 double geon_tanh(double x) {
-  if (std::isnan(x)) return x;
-  const double a = std::fabs(x);
-  double t;
-  if (!(a < 22.0)) {
-    t = 1.0;
-  } else if (a < 0x1p-28) {
-    return x;
-  } else {
-    const double e = geon_expm1_pos(2.0 * a);
-    t = e / (e + 2.0);
+  const uint32_t jx = gm_hi_word(x), ix = jx & 0x7fffffffu;
+  const bool neg = (jx >> 31) != 0;
+  if (ix >= 0x7ff00000u) return neg ? 1.0 / x - 1.0 : 1.0 / x + 1.0;
+  double z = 1.0;
+  if (ix < 0x40360000u) {
+    if (ix < 0x3c800000u) return x * (1.0 + x);
+    if (ix >= 0x3ff00000u) {
+      const double m = geon_expm1(2.0 * std::fabs(x));
+      z = 1.0 - 2.0 / (m + 2.0);
+    } else {
+      const double m = geon_expm1(-2.0 * std::fabs(x));
+      z = -m / (m + 2.0);
+    }
   }
-  return std::copysign(t, x);
+  return neg ? -z : z;
 }
 
 struct MathLibm {

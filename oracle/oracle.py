@@ -74,6 +74,13 @@ def geon_tanh(x):
     return o
 
 
+def geon_expm1(x):
+    x, xp = _d(x)
+    o = np.empty_like(x)
+    lib().orc_geon_expm1(xp, ctypes.c_int64(x.size), _p(o, ctypes.c_double))
+    return o
+
+
 def inv4(m):
     m, mp = _d(m)
     o = np.empty(16)

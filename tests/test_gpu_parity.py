@@ -197,6 +197,29 @@ def test_render_vs_libm_reference(geon, orc):
     assert np.median(err) <= 1e-12
 
 
+@pytest.mark.parametrize("params", [ALC_CFG3[1], ALC_DEF[1]], ids=["alcubierre_sigma8", "alcubierre_default"])
+def test_alcubierre_equals_libm_reference(geon, orc, params):
+    """tanh follows the libm's own method, so the Alcubierre path (tanh, sqrt and
+    IEEE arithmetic only) equals the reference run with glibc bit for bit: the
+    curvature chain, the grid job and the FP64 trace."""
+    m = geon.Alcubierre(*params)
+    x = sample_points(2, 40, 77)
+    for what, fn in [("riemann", geon.curvature.riemann), ("einstein", geon.curvature.einstein),
+                     ("stress_energy", geon.curvature.stress_energy)]:
+        assert np.array_equal(fn(m, x), orc.curvature(2, params, x, what, math=LIBM)), what
+    pts, ein, nec, k = geon.curvature.grid(m, (-4.0, -4.0, -4.0), (4.0, 4.0, 4.0), (9, 7, 5), nk=4, seed=3,
+                                           with_k=True)
+    assert np.array_equal(ein, orc.curvature(2, params, pts, "einstein", math=LIBM))
+    assert np.array_equal(nec, orc.nec(2, params, pts, k, math=LIBM), equal_nan=True)
+    obs, fov, fs = camera_for(2)
+    cam = geon.Camera(obs, fov, 24, 24, forward_sign=fs)
+    y0 = cam.ray_states(cam.tetrad(m))
+    res = geon.trace(m, y0, 0.05, 3000)
+    term, yf, steps, resid = orc.trace(2, params, y0, 0.05, 3000, math=LIBM)
+    assert np.array_equal(res.termination, term) and np.array_equal(res.steps_taken, steps)
+    assert np.array_equal(res.final_state, yf)
+
+
 def test_sky_sample_matches(geon, orc):
     rng = np.random.default_rng(7)
     d = rng.normal(size=(200000, 3))

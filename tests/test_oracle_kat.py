@@ -6,6 +6,7 @@ bin/validate_shadow.rs (quoted in README.md:43-50). tests/golden/ holds those
 numbers; the oracle must reproduce every printed digit.
 """
 import json
+import math
 import os
 
 import numpy as np
@@ -94,9 +95,16 @@ def test_geon_math_close_to_libm(orc):
     assert us.max() <= 1 and uc.max() <= 1
     assert (us == 0).mean() > 0.97 and (uc == 0).mean() > 0.97
     assert c[-2] == np.cos(np.pi / 2)  # 6.123233995736766e-17, as glibc
-    t = rng.uniform(-25, 25, 100000)
-    ut = np.abs(orc.geon_tanh(t).view(np.int64) - np.tanh(t).view(np.int64))
-    assert ut.max() <= 3
+    # tanh (and expm1) follow the libm's own method: equal bit for bit
+    t = np.concatenate([rng.uniform(-25, 25, 100000), rng.uniform(-1.2, 1.2, 100000),
+                        np.ldexp(rng.uniform(-1, 1, 20000), -rng.integers(0, 60, 20000)),
+                        [0.0, -0.0, 22.0, -22.0, 1.0, -1.0, np.inf, -np.inf]])
+    # (math.tanh is the platform libm's; numpy's tanh is its own SIMD code)
+    libm_tanh = np.array([math.tanh(v) for v in t])
+    assert np.array_equal(orc.geon_tanh(t).view(np.int64), libm_tanh.view(np.int64))
+    e = np.concatenate([rng.uniform(-50, 50, 100000), rng.uniform(-2, 2, 100000), [0.0, 709.0, -800.0]])
+    libm_expm1 = np.array([math.expm1(v) for v in e])
+    assert np.array_equal(orc.geon_expm1(e).view(np.int64), libm_expm1.view(np.int64))
 
 
 def test_math_mode_floor(orc):
