@@ -167,7 +167,7 @@ def main():
     ap.add_argument("--cpu-rays", type=int, default=4096)
     ap.add_argument("--bisect-rays", type=int, default=BISECT_RAYS,
                     help="speculative bisection width (rays per round over all brackets)")
-    ap.add_argument("--reserve", type=int, default=RESERVE,
+    ap.add_argument("--reserve", type=float, default=RESERVE,
                     help="block slots per SM the sweep leaves free for the bisections (latency vs throughput)")
     ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy leg traces every k-th sweep ray")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 leg, accuracy, e2e and CPU legs")
@@ -229,7 +229,7 @@ def main():
         sa.wait_stream(main)
         sb.wait_stream(main)
         ea0.record(sa)
-        lib.geon_set_persistent_reserve(args.reserve)  # leave room on every SM for the bisection rounds
+        lib.geon_set_persistent_reserve_f(args.reserve)  # leave room on every SM for the bisection rounds
         check(lib.geon_shadow_classify_dev(h, R_OBS, s_alpha.data_ptr(), s_n, STEP, MAX_STEPS, precision,
                                            d_term.data_ptr(), d_steps.data_ptr(), sa.cuda_stream))
         lib.geon_set_persistent_reserve(0)

@@ -119,6 +119,7 @@ SIGNATURES = {
     "geon_get_mixed_band": (ctypes.c_double, [ctypes.c_int]),
     "geon_set_mixed_reproject": (None, [ctypes.c_int]),
     "geon_set_persistent_reserve": (None, [ctypes.c_int]),
+    "geon_set_persistent_reserve_f": (None, [ctypes.c_double]),
     "geon_set_mixed_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "geon_get_mixed_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "geon_autotune_mixed": (ctypes.c_int, [c_void_p, ctypes.c_int64, ctypes.c_int64, c_double_p,

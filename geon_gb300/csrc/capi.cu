@@ -29,7 +29,7 @@ std::atomic<int> g_show_stars{1};
 // M, b0, s; 0 disables) and the null re-projection switch.
 std::atomic<float> g_band[4] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
 std::atomic<int> g_reproject{0};
-std::atomic<int> g_reserve{0};
+std::atomic<float> g_reserve{0.0f};
 std::atomic<double> g_rtol{1e-10};  // GEON_ADAPTIVE error tolerances
 std::atomic<double> g_atol{1e-12};
 // Mixed-kernel variant per metric kind and ray source (camera/array, equatorial),
@@ -269,7 +269,10 @@ void geon_get_adaptive_tolerance(double* rtol, double* atol) {
   if (atol) *atol = g_atol.load();
 }
 
-void geon_set_persistent_reserve(int blocks_per_sm) { g_reserve.store(blocks_per_sm < 0 ? 0 : blocks_per_sm); }
+void geon_set_persistent_reserve(int blocks_per_sm) { geon_set_persistent_reserve_f((double)blocks_per_sm); }
+void geon_set_persistent_reserve_f(double blocks_per_sm) {
+  g_reserve.store(blocks_per_sm > 0.0 ? (float)blocks_per_sm : 0.0f);  // NaN and negatives: none
+}
 
 int geon_set_mixed_variant(int kind, int source, int variant) {
   if (kind < GEON_MINKOWSKI || kind > GEON_MORRIS_THORNE || source < 0 || source > 1 || variant < 0 ||

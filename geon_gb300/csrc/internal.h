@@ -89,7 +89,7 @@ struct TraceLaunch {
   float diverged_rgb[3];  // RenderConfig::diverged_rgb (render.rs:25)
   // mixed precision
   float band;          // FP64 band half-width in the metric's own scale (0 = no band)
-  int reserve_per_sm;  // persistent grid leaves this many blocks per SM free
+  float reserve_per_sm;  // persistent grid leaves this many blocks per SM free (may be fractional)
   int variant;         // mixed kernel register-cap variant (0: none, 1: 5 blocks/SM, 2: 6)
   int mixed_flags;     // MIXED_* bits
   // adaptive stepping (GEON_ADAPTIVE): error tolerances
@@ -104,6 +104,16 @@ cudaError_t launch_trace_fp64(const TraceLaunch& L, int src, int sink, cudaStrea
 // ---- launchers (trace_mixed.cu) ----
 cudaError_t launch_trace_mixed(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 // ---- launchers (trace_adaptive.cu) ----
+// Blocks of a persistent grid: every resident slot (sms x per_sm) minus the
+// slots per SM the caller keeps free for a concurrent job; a fractional reserve
+// is rounded over the whole GPU (some SMs keep one slot more than others). At
+// least one block per SM.
+inline int64_t persistent_slots(int sms, int per_sm, float reserve) {
+  double use = (double)per_sm - (double)reserve;
+  if (use < 1.0) use = 1.0;
+  return (int64_t)((double)sms * use);
+}
+
 cudaError_t launch_trace_adaptive(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 // rgb and rgb8 (the tonemapped bytes) may each be null
 cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,

@@ -150,8 +150,7 @@ static cudaError_t launch_ka(const TraceLaunch& L, cudaStream_t s) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_adaptive_kernel<K, SRC, SINK>, TRACE_BLOCK, 0);
     per_sm = occ < 1 ? 1 : occ;
   }
-  const int use = per_sm - L.reserve_per_sm < 1 ? 1 : per_sm - L.reserve_per_sm;
-  int64_t blocks = (int64_t)sms * use;
+  int64_t blocks = persistent_slots(sms, per_sm, L.reserve_per_sm);
   const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;

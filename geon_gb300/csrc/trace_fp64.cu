@@ -131,8 +131,7 @@ static cudaError_t launch_kst(const TraceLaunch& L, cudaStream_t s) {
   }
   // persistent grid: every resident slot, minus the blocks per SM the caller
   // keeps free for a concurrent job
-  const int use = per_sm - L.reserve_per_sm < 1 ? 1 : per_sm - L.reserve_per_sm;
-  const int64_t slots = (int64_t)sms * use;
+  const int64_t slots = persistent_slots(sms, per_sm, L.reserve_per_sm);
   const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
   int grid = (int)(need < slots ? need : slots);
   if (grid < 1) grid = 1;

@@ -222,6 +222,10 @@ void geon_get_adaptive_tolerance(double* rtol, double* atol);
  * to a sweep), calls made after this keep `blocks_per_sm` resident slots per SM
  * free. Default 0. */
 void geon_set_persistent_reserve(int blocks_per_sm);
+/* The same with a fractional count: the grid keeps floor(SMs x (occupancy -
+ * blocks_per_sm)) blocks, so e.g. 4.5 leaves 4 slots on half of the SMs and 5
+ * on the others. No counterpart in the reference (no persistent kernels). */
+void geon_set_persistent_reserve_f(double blocks_per_sm);
 /* Register-cap variant of the mixed kernel per metric kind and ray source
  * (source 0: camera rays and ray arrays, 1: equatorial shadow rays): 0 = no
  * cap, 1 = fit 8 blocks of 128 threads per SM, 2 = fit 10. geon_autotune_mixed
