@@ -74,9 +74,10 @@ __device__ __forceinline__ void rhs_planar_schw(const AConsts<float>& C, float r
   const float f = Mt::fma(-C.two_m, ir, 1.0f);
   const float A = C.m * ir * ir;
   const float gtr = Mt::div(A, f);
-  *k4 = -2.0f * gtr * p0 * p1;
+  const float u = -2.0f * p1;  // shared by Gamma^t_tr and Gamma^ph_rph terms
+  *k4 = (u * gtr) * p0;
   *k5 = Mt::fma(-A * f, p0 * p0, Mt::fma(gtr, p1 * p1, (r - C.two_m) * (p3 * p3)));
-  *k7 = -2.0f * p3 * (ir * p1);
+  *k7 = (u * ir) * p3;
 }
 
 template <int K, int FEAT = 0>
@@ -262,9 +263,14 @@ struct MixedStepper {
     fast_two_sum_update(hi[0], lo[0], i0);
     fast_two_sum_update(hi[1], lo[1], i1);
     fast_two_sum_update(hi[3], lo[3], i3);
-    two_sum_update(hi[4], lo[4], i4);
+    // p^t = E/f and p^phi = L/r^2 keep their sign and change by a small
+    // fraction per step (|inc/p^phi| = 2h|p^r|/r; |inc/p^t| = 2h m |p^r|/(r^2 f),
+    // below 0.1 down to r = 2.1M and below 1 down to ~2.01M, one or two steps
+    // before the capture radius), so Fast2Sum is exact for them wherever the
+    // ray's class is still open; p^r crosses zero at periapsis and keeps TwoSum.
+    fast_two_sum_update(hi[4], lo[4], i4);
     two_sum_update(hi[5], lo[5], i5);
-    two_sum_update(hi[7], lo[7], i7);
+    fast_two_sum_update(hi[7], lo[7], i7);
     if ((++nsteps & 7) == 0) {
       renormalise(hi[0], lo[0]);
       renormalise(hi[1], lo[1]);
