@@ -45,9 +45,9 @@ SCHW = [1.0, 1.001, 1000.0]
 # Block slots per SM the persistent sweep grid leaves to the concurrent bisection
 # rounds. The bisection is a chain of dependent rounds (latency-bound), the sweep
 # throughput-bound: with 8 resident blocks per SM (the planar equatorial step,
-# 64 registers) and 16 steps per refill, leaving 5 balances the two (measured on
+# 63-64 registers) and 16 steps per refill, leaving 5 balances the two (measured on
 # GB300 at 16384 rays per round: 4 -> 1.39e11, 5 -> 1.43e11 ray-steps/s; sweep /
-# bisection 463 / 362 ms at 5, 439 / 475 ms at 4).
+# bisection 463 / 362 ms at 5, 439 / 475 ms at 4; fractional 4.25-4.75 slower).
 RESERVE = 5
 BISECT_RAYS = 16384  # speculative width of a bisection round (geon_set_bisect_rays_per_round)
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
