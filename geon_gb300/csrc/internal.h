@@ -90,7 +90,7 @@ struct TraceLaunch {
   // mixed precision
   float band;          // FP64 band half-width in the metric's own scale (0 = no band)
   float reserve_per_sm;  // persistent grid leaves this many blocks per SM free (may be fractional)
-  int variant;         // mixed kernel register-cap variant (0: none, 1: 5 blocks/SM, 2: 6)
+  int variant;         // mixed kernel register-cap variant (0: none, 1: 8 blocks/SM, 2: 10)
   int mixed_flags;     // MIXED_* bits
   // adaptive stepping (GEON_ADAPTIVE): error tolerances
   double rtol, atol;

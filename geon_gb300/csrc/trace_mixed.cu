@@ -365,9 +365,9 @@ struct MixedStepper {
 };
 
 // MINB is the register cap chosen by the autotuner: __launch_bounds__(128, MINB)
-// asks the compiler to fit MINB blocks per SM (1: no cap, 72 registers for the
-// Schwarzschild step, 7 blocks; 8: <= 64 registers; 10: <= 51), trading
-// registers (and spills) for resident warps.
+// asks the compiler to fit MINB blocks per SM (1: no cap, 63 registers and 8
+// blocks for the planar equatorial step, 72 and 7 for the camera step; 8: <= 64
+// registers; 10: <= 51), trading registers (and spills) for resident warps.
 template <int K, int SRC, int SINK, int MINB, int FEAT>
 __global__ void __launch_bounds__(TRACE_BLOCK, MINB) trace_mixed_kernel(const TraceLaunch L) {
   constexpr int PL = (SRC == SRC_EQUATORIAL && K == KIND_SCHWARZSCHILD) ? FEAT_PLANAR : 0;
