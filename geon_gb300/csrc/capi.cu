@@ -29,6 +29,7 @@ std::atomic<int> g_show_stars{1};
 // M, b0, s; 0 disables) and the null re-projection switch.
 std::atomic<float> g_band[4] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
 std::atomic<int> g_reproject{0};
+std::atomic<int> g_orbit{0};
 std::atomic<float> g_reserve{0.0f};
 std::atomic<double> g_rtol{1e-10};  // GEON_ADAPTIVE error tolerances
 std::atomic<double> g_atol{1e-12};
@@ -140,7 +141,7 @@ TraceLaunch base_launch(geon_metric_t m, double step, int64_t max_steps) {
   L.sixth = step / 6.0;
   L.max_steps = max_steps;
   L.band = g_band[m->desc.kind].load();
-  L.mixed_flags = g_reproject.load() ? MIXED_REPROJECT : 0;
+  L.mixed_flags = (g_reproject.load() ? MIXED_REPROJECT : 0) | (g_orbit.load() ? MIXED_ORBIT : 0);
   L.reserve_per_sm = g_reserve.load();
   L.variant = g_variant[m->desc.kind][0].load();
   L.rtol = g_rtol.load();
@@ -246,6 +247,8 @@ double geon_get_mixed_band(int kind) {
 }
 
 void geon_set_mixed_reproject(int on) { g_reproject.store(on ? 1 : 0); }
+void geon_set_mixed_orbit_plane(int on) { g_orbit.store(on ? 1 : 0); }
+int geon_get_mixed_orbit_plane(void) { return g_orbit.load(); }
 
 int geon_set_bisect_rays_per_round(int64_t rays) {
   if (rays < 1 || rays > ((int64_t)1 << 24)) return fail(GEON_ERR_INVALID, "rays per round out of range");

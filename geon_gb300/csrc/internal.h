@@ -49,7 +49,7 @@ struct CameraDesc {
   int forward_sign;
 };
 
-enum : int { MIXED_REPROJECT = 1 };
+enum : int { MIXED_REPROJECT = 1, MIXED_ORBIT = 2 };
 constexpr int MIXED_VARIANTS = 3;
 
 // A regular grid of points for curvature jobs (geon_grid of the ABI).

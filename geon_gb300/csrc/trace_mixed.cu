@@ -59,25 +59,88 @@ __device__ __forceinline__ bool ff_gt(float hi, float lo, float thi, float tlo) 
 // leave both out, which keeps their register demand (and code) small.
 // FEAT_PLANAR: every ray is an equatorial Schwarzschild ray (theta = pi/2,
 // p^theta = 0, bin/validate_shadow.rs:20-35); FEAT_PLANAR_DYN: a per-ray flag
-// says so (the serving kernel, whose lanes take rays of any job).
-enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2, FEAT_PLANAR = 4, FEAT_PLANAR_DYN = 8 };
+// says so (the serving kernel, whose lanes take rays of any job). FEAT_ORBIT
+// (opt-in, MIXED_ORBIT): rays of a spherically symmetric metric (Schwarzschild,
+// Morris-Thorne) are turned into the frame of their own orbit plane at load,
+// stepped there on the equator, and turned back at the end.
+enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2, FEAT_PLANAR = 4, FEAT_PLANAR_DYN = 8, FEAT_ORBIT = 16 };
 
-// Schwarzschild right-hand side on the equatorial plane: rhs_stage at
-// sin theta = 1, cos theta = 0, p^theta = 0, where its theta terms vanish
-// (Gamma^th_phph = -sin cos, Gamma^ph_thph p^th, p^th p^th) and what remains is
-// evaluated with the same operations. The plane is invariant under the
-// geodesic equation, so a ray that starts in it stays in it.
-__device__ __forceinline__ void rhs_planar_schw(const AConsts<float>& C, float r, float p0, float p1, float p3,
-                                                float* k4, float* k5, float* k7) {
+// Right-hand side on the equatorial plane: rhs_stage at sin theta = 1,
+// cos theta = 0, p^theta = 0, where its theta terms vanish (Gamma^th_phph =
+// -sin cos, Gamma^ph_thph p^th, p^th p^th) and what remains is evaluated with
+// the same operations. The plane is invariant under the geodesic equation, so
+// a ray that starts in it stays in it. Schwarzschild (r) and Morris-Thorne (l).
+template <int K>
+__device__ __forceinline__ void rhs_planar(const AConsts<float>& C, float r, float p0, float p1, float p3,
+                                           float* k4, float* k5, float* k7) {
   using Mt = AMath<float>;
+  const float u = -2.0f * p1;  // shared by the Gamma^t_tr and Gamma^ph_rph terms
+  if (K == KIND_MORRIS_THORNE) {
+    const float q = Mt::div(r, Mt::fma(r, r, C.b0sq));  // Gamma^ph_lph = l / (b0^2 + l^2)
+    *k4 = 0.0f;
+    *k5 = r * (p3 * p3);
+    *k7 = (u * q) * p3;
+    return;
+  }
   const float ir = Mt::rcp(r);
   const float f = Mt::fma(-C.two_m, ir, 1.0f);
   const float A = C.m * ir * ir;
   const float gtr = Mt::div(A, f);
-  const float u = -2.0f * p1;  // shared by Gamma^t_tr and Gamma^ph_rph terms
   *k4 = (u * gtr) * p0;
   *k5 = Mt::fma(-A * f, p0 * p0, Mt::fma(gtr, p1 * p1, (r - C.two_m) * (p3 * p3)));
   *k7 = (u * ir) * p3;
+}
+
+// The frame of a ray's orbit plane (spherically symmetric metrics). With the
+// radial unit vector n = (sin th cos ph, sin th sin ph, cos th) and its rate
+// w = p^th e_th + p^ph sin th e_ph, the ray moves in the plane of n and w; in
+// the basis (e1 = n, e2 = w / |w|, e1 x e2) it starts at theta' = pi/2,
+// phi' = 0 with p^theta' = 0 and p^phi' = |w|, while t, r and their momenta are
+// unchanged. A radial ray (w = 0) takes e2 = e_th and p^phi' = 0.
+__device__ __forceinline__ void orbit_in(const double y[8], double yr[8], float e1[3], float e2[3]) {
+  double st, ct, sp, cp;
+  ::sincos(y[2], &st, &ct);
+  ::sincos(y[3], &sp, &cp);
+  const double n[3] = {st * cp, st * sp, ct};
+  const double et[3] = {ct * cp, ct * sp, -st};
+  const double ep[3] = {-sp, cp, 0.0};
+  double w[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) w[i] = y[6] * et[i] + y[7] * st * ep[i];
+  const double wn = ::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  const bool turning = wn > 0.0 && isfinite(wn);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    e1[i] = (float)n[i];
+    e2[i] = (float)(turning ? w[i] / wn : et[i]);
+  }
+  yr[0] = y[0]; yr[1] = y[1]; yr[2] = 1.5707963267948966; yr[3] = 0.0;
+  yr[4] = y[4]; yr[5] = y[5]; yr[6] = 0.0; yr[7] = turning ? wn : 0.0;
+}
+
+// Back from the orbit-plane frame: theta, phi from the final radial direction
+// n = cos phi' e1 + sin phi' e2 (phi in (-pi, pi]: the orbit frame does not
+// count turns), and p^theta, p^phi from its rate p^phi' (-sin phi' e1 + cos
+// phi' e2).
+__device__ __forceinline__ void orbit_out(const double yr[8], const float e1[3], const float e2[3], double y[8]) {
+  double sf, cf;
+  ::sincos(yr[3], &sf, &cf);
+  double n[3], w[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    n[i] = cf * (double)e1[i] + sf * (double)e2[i];
+    w[i] = yr[7] * (cf * (double)e2[i] - sf * (double)e1[i]);
+  }
+  const double nn = ::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  const double nz = fmin(1.0, fmax(-1.0, n[2] / nn));
+  const double th = ::acos(nz), ph = ::atan2(n[1], n[0]);
+  double st, ct, sp, cp;
+  ::sincos(th, &st, &ct);
+  ::sincos(ph, &sp, &cp);
+  y[0] = yr[0]; y[1] = yr[1]; y[2] = th; y[3] = ph;
+  y[4] = yr[4]; y[5] = yr[5];
+  y[6] = w[0] * ct * cp + w[1] * ct * sp - w[2] * st;
+  y[7] = (w[1] * cp - w[0] * sp) / st;
 }
 
 template <int K, int FEAT = 0>
@@ -90,6 +153,7 @@ struct MixedStepper {
   unsigned nsteps = 0;  // steps this ray has taken: renormalisation follows the ray, not the lane
   bool ready = false;
   bool planar = (FEAT & FEAT_PLANAR) != 0;
+  float oe1[3], oe2[3];  // orbit-plane frame (FEAT_ORBIT only)
 
   // Serving: the source of the ray just loaded (equatorial rays step on the plane).
   __device__ __forceinline__ void set_source(int src) {
@@ -121,12 +185,25 @@ struct MixedStepper {
   __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) {
     if (!ready) setup(L);
     nsteps = 0;
-    load_state(y0);
+    if constexpr ((FEAT & FEAT_ORBIT) != 0) {
+      double yr[8];
+      orbit_in(y0, yr, oe1, oe2);
+      load_state(yr);
+    } else {
+      load_state(y0);
+    }
   }
 
   __device__ __forceinline__ void to_double(double out[8]) const {
+    if constexpr ((FEAT & FEAT_ORBIT) != 0) {
+      double yr[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) out[i] = (double)hi[i] + (double)lo[i];
+      for (int i = 0; i < 8; ++i) yr[i] = (double)hi[i] + (double)lo[i];
+      orbit_out(yr, oe1, oe2, out);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) out[i] = (double)hi[i] + (double)lo[i];
+    }
   }
 
   // Termination tests of the reference, evaluated on the compensated state.
@@ -220,14 +297,15 @@ struct MixedStepper {
     return STEP_OK;
   }
 
-  // step_fp32 for an equatorial Schwarzschild ray: the six components that
-  // move (t, r, phi and their momenta), theta and p^theta held at their loaded
-  // values (pi/2 and 0). Same stage points, horizon rule, compensated update
-  // and renormalisation as step_fp32.
+  // step_fp32 for a ray on the equator (Schwarzschild: equatorial rays, or any
+  // ray in its orbit-plane frame; Morris-Thorne in its orbit-plane frame): the
+  // six components that move (t, r or l, phi and their momenta), theta and
+  // p^theta held at their loaded values (pi/2 and 0). Same stage points,
+  // horizon rule, compensated update and renormalisation as step_fp32.
   __device__ __forceinline__ int step_fp32_planar(const TraceLaunch& L) {
     float k1, k4, k5, k7;
     float p0 = hi[4], p1 = hi[5], p3 = hi[7];
-    rhs_planar_schw(C, hi[1], p0, p1, p3, &k4, &k5, &k7);
+    rhs_planar<K>(C, hi[1], p0, p1, p3, &k4, &k5, &k7);
     k1 = p1;
     float a0 = p0, a1 = p1, a3 = p3, a4 = k4, a5 = k5, a7 = k7;
     float k0 = p0, k3 = p3;
@@ -240,7 +318,7 @@ struct MixedStepper {
       p3 = __fmaf_rn(c, k7, hi[7]);
       const float r = __fmaf_rn(c, k1, hi[1]);
       rmin = st == 0 ? r : fminf(rmin, r);
-      rhs_planar_schw(C, r, p0, p1, p3, &k4, &k5, &k7);
+      rhs_planar<K>(C, r, p0, p1, p3, &k4, &k5, &k7);
       k0 = p0; k1 = p1; k3 = p3;
       if (st < 2) {
         a0 = __fmaf_rn(2.0f, k0, a0);
@@ -251,7 +329,7 @@ struct MixedStepper {
         a7 = __fmaf_rn(2.0f, k7, a7);
       }
     }
-    if (!(rmin > C.two_m)) return STEP_HORIZON;
+    if (K == KIND_SCHWARZSCHILD && !(rmin > C.two_m)) return STEP_HORIZON;
     const float i0 = sixth * (a0 + k0), i1 = sixth * (a1 + k1), i3 = sixth * (a3 + k3);
     const float i4 = sixth * (a4 + k4), i5 = sixth * (a5 + k5), i7 = sixth * (a7 + k7);
     // NaN guard on the momenta: every stage value of p^t, p^r, p^phi enters
@@ -337,6 +415,7 @@ struct MixedStepper {
   __device__ __forceinline__ int step(const TraceLaunch& L) {
     if ((FEAT & FEAT_BAND) && K != KIND_MINKOWSKI && L.band > 0.0f && in_band<K>(L.M, hi[1], hi[2], hi[3], L.band))
       return step_fp64(L);
+    if ((FEAT & FEAT_ORBIT) && (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE)) return step_fp32_planar(L);
     if (K == KIND_SCHWARZSCHILD && (FEAT & (FEAT_PLANAR | FEAT_PLANAR_DYN)) && ((FEAT & FEAT_PLANAR) || planar))
       return step_fp32_planar(L);
     return step_fp32(L);
@@ -398,6 +477,11 @@ template <int K, int SRC, int SINK>
 static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
   const int feat = ((K != KIND_MINKOWSKI && L.band > 0.0f) ? FEAT_BAND : 0) |
                    ((L.mixed_flags & MIXED_REPROJECT) ? FEAT_REPROJECT : 0);
+  if constexpr ((K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) && SRC == SRC_CAMERA && SINK == SINK_RENDER) {
+    // orbit-plane frame (opt-in): renders only, whose sink needs the escape
+    // direction, not the unwrapped final phi
+    if (feat == 0 && (L.mixed_flags & MIXED_ORBIT)) return launch_mst_v<K, SRC, SINK, 1, FEAT_ORBIT>(L, s);
+  }
   switch (feat) {  // the optional parts run without a register cap
     case FEAT_BAND: return launch_mst_v<K, SRC, SINK, 1, FEAT_BAND>(L, s);
     case FEAT_REPROJECT: return launch_mst_v<K, SRC, SINK, 1, FEAT_REPROJECT>(L, s);

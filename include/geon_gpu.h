@@ -205,6 +205,14 @@ int geon_get_show_stars(void);
 int geon_set_mixed_band(int kind, double band);
 double geon_get_mixed_band(int kind);
 void geon_set_mixed_reproject(int on);
+/* Opt-in (default off): mixed-precision renders of the spherically symmetric
+ * metrics (Schwarzschild, Morris-Thorne) trace each camera ray in the frame of
+ * its own orbit plane, on the equator with no trigonometry in the step, and
+ * turn its final state back for the sky lookup. Same geodesics; not the
+ * default mixed step's bits. Renders only (the frame does not count turns of
+ * phi); not applied to served requests. No counterpart in the reference. */
+void geon_set_mixed_orbit_plane(int on);
+int geon_get_mixed_orbit_plane(void);
 /* Error tolerances of GEON_ADAPTIVE: a step is accepted when
  * sqrt(mean_i((e_i / (atol + rtol * max(|y_i|, |y_new_i|)))^2)) <= 1.
  * Defaults rtol 1e-10, atol 1e-12. Calls made after this use them. */
@@ -330,8 +338,8 @@ int geon_shadow_bisect_dev_noalloc(geon_metric_t schwarzschild, double r_obs, co
  * Each result is the one the matching single-call entry point gives
  * (geon_render_ex, geon_shadow_bisect with one bracket, geon_curvature_grid),
  * bit for bit, whatever else runs beside it. Mixed-precision requests run the
- * default mixed step (geon_set_mixed_band / geon_set_mixed_reproject are not
- * applied to served requests). */
+ * default mixed step (geon_set_mixed_band / geon_set_mixed_reproject /
+ * geon_set_mixed_orbit_plane are not applied to served requests). */
 typedef struct geon_server* geon_server_t;
 enum geon_job_type { GEON_JOB_RENDER = 0, GEON_JOB_BISECT = 1, GEON_JOB_CURVATURE = 2 };
 
