@@ -125,3 +125,19 @@ def test_server_tuning_argument_errors_without_gpu(lib):
     assert lib.geon_server_set_steps_per_launch(None, 1, 4096) == -1
     assert lib.geon_server_get_steps_per_launch(None, 1) == -1
     assert lib.geon_server_autotune(None, None, None) == -1
+
+
+def test_mixed_orbit_plane_flag_without_gpu(lib):
+    assert lib.geon_get_mixed_orbit_plane() == 0  # off by default
+    lib.geon_set_mixed_orbit_plane(1)
+    assert lib.geon_get_mixed_orbit_plane() == 1
+    lib.geon_set_mixed_orbit_plane(0)
+    assert lib.geon_get_mixed_orbit_plane() == 0
+
+
+def test_persistent_reserve_setters_without_gpu(lib):
+    # plain stores, no CUDA: whole and fractional counts, and values that mean none
+    for v in (0.0, 4.5, -1.0, float("nan"), 1e30):
+        lib.geon_set_persistent_reserve_f(v)
+    lib.geon_set_persistent_reserve(3)
+    lib.geon_set_persistent_reserve(0)
