@@ -605,6 +605,31 @@ def exotic_main(args):
           {"exotic": out, "timing": "host API wall time"})
 
 
+def curvature_cpu_leg(orc, params, pts, threads, budget_s=8.0):
+    """The config-4 job per grid point (Einstein tensor + T(k, k) for 16 null
+    vectors) on the oracle, on a uniform sample of the grid sized to about
+    budget_s each: once with the reference's call graph (Riemann formed again
+    inside every curvature.rs call: twice for the Einstein tensor, twice per
+    vector for T(k, k)) and once with Riemann formed once per point (the same
+    bits). The cost does not depend on the vectors' values, so 16 copies of the
+    reference's own k = (1, 1, 0, 0) stand in for them."""
+    k = np.tile([[1.0, 1.0, 0.0, 0.0]], (16, 1))
+    out = {}
+    for name, faithful in (("reference_call_graph", True), ("riemann_once", False)):
+        def run(m):
+            sub = pts[np.linspace(0, len(pts) - 1, m).astype(np.int64)]
+            t0 = time.perf_counter()
+            orc.curvature(2, params, sub, "einstein", math=orc.LIBM, faithful=faithful, nthreads=threads)
+            orc.nec(2, params, sub, k, math=orc.LIBM, faithful=faithful, nthreads=threads)
+            return time.perf_counter() - t0
+        m = min(len(pts), 256)
+        dt = run(m)
+        m = int(min(len(pts), max(m, m * budget_s / max(dt, 1e-6))))
+        dt = run(m)
+        out[name] = {"value": m / dt, "points": m, "seconds": dt}
+    return out
+
+
 def curvature_main(args):
     """Curvature grid jobs (FP64): 128^3 Alcubierre (v_s 0.5, R 2, sigma 8)
     Einstein + T(k,k) for 16 null vectors per point; a 4096-point Morris-Thorne
@@ -625,6 +650,7 @@ def curvature_main(args):
     oein_libm = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.LIBM, nthreads=threads)
     err_libm = float(np.max(np.abs(oein_libm.reshape(-1, 16) - ein[sub].reshape(-1, 16))))
     bit_exact_libm = bool(np.array_equal(oein_libm.reshape(-1, 16), ein[sub].reshape(-1, 16)))
+    cpu = curvature_cpu_leg(orc, [2.0, 0.125, 0.5, 0.0], pts, threads)
     # Kernel-only leg: the same grid job through the device-pointer entry
     # point, outputs resident in HBM (537 MB at 128^3, larger than L2), CUDA
     # events on the launching stream.
@@ -669,8 +695,11 @@ def curvature_main(args):
                                                 "T_tt_throat_check": "tests/test_gpu_curvature_grid.py"},
                          "schwarzschild_vacuum": {"points": 100000, "ms": 1e3 * dt_s, "points_per_s": 1e5 / dt_s,
                                                   "max_abs_ricci_scalar": float(np.max(np.abs(rs)))}},
-           "cpu_baseline": {"value": len(sub) / dt_cpu, "unit": "grid-points/s", "cores": threads, "kind": "port",
-                            "sample": f"{len(sub)} grid points, einstein only ({dt_cpu:.1f} s)"},
+           "cpu_baseline": {"value": cpu["reference_call_graph"]["value"], "unit": "grid-points/s", "cores": threads,
+                            "kind": "port",
+                            "sample": (f"{cpu['reference_call_graph']['points']} grid points, Einstein + 16 T(k,k) each, "
+                                       f"curvature.rs call graph ({cpu['reference_call_graph']['seconds']:.1f} s)"),
+                            "riemann_once": cpu["riemann_once"]},
            "timing": "host API wall time (includes the copy of results to the host)"})
 
 

@@ -23,3 +23,18 @@ def test_reference_arm_contract_line():
     assert d["steps"] == 1 and d["warmup"] == 3 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "ray-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_curvature_cpu_leg(orc):
+    """The config-4 CPU baseline times the oracle with the reference's call
+    graph (Riemann again inside every call) and with Riemann once; the former
+    does ~17x the Riemann work per point."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from geon_gb300.curvature import grid_points
+    pts = grid_points((-4, -4, -4), (4, 4, 4), (32, 32, 32))
+    r = bench.curvature_cpu_leg(orc, [2.0, 0.125, 0.5, 0.0], pts, orc.hardware_threads(), budget_s=0.3)
+    assert set(r) == {"reference_call_graph", "riemann_once"}
+    for v in r.values():
+        assert v["value"] > 0 and 256 <= v["points"] <= len(pts) and v["seconds"] > 0
+    assert r["riemann_once"]["value"] > 3 * r["reference_call_graph"]["value"]
