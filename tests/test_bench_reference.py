@@ -28,7 +28,7 @@ def test_reference_arm_contract_line():
 def test_curvature_cpu_leg(orc):
     """The config-4 CPU baseline times the oracle with the reference's call
     graph (Riemann again inside every call) and with Riemann once; the former
-    does ~17x the Riemann work per point."""
+    forms Riemann 34 times per point (2 for the Einstein tensor, 2 per vector)."""
     sys.path.insert(0, ROOT)
     import bench
     from geon_gb300.curvature import grid_points
