@@ -324,7 +324,7 @@ def main():
         "metric": "ray-steps/s", "value": value, "unit": "ray-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 with f64 band (mixed)" if prec == 1 else "f64",
+        "dtype": "f32 (mixed: FP32 right-hand side, compensated f32-pair state)" if prec == 1 else "f64",
         "data": "synthetic (seeded alpha and brackets)",
         "config": {"workload": "schwarzschild shadow sweep: 2^20 equatorial rays alpha~U[10,20] deg + 64 concurrent "
                                "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
@@ -808,7 +808,7 @@ def serve_main(args):
     line = {"metric": "ray-steps/s", "value": out[main_prec]["ray_steps_per_s"], "unit": "ray-steps/s",
             "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * legs[main_prec]["drain_wall_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 with f64 band (mixed)" if main_prec == "mixed" else "f64",
+            "dtype": "f32 (mixed: FP32 right-hand side, compensated f32-pair state)" if main_prec == "mixed" else "f64",
             "data": "synthetic seeded request stream",
             "config": {"workload": f"serving stream: {len(reqs)} requests, Poisson mean {args.rate}/s "
                                    f"({n_types['render']} renders 128^2-2048^2 over 4 metrics, "
