@@ -31,6 +31,7 @@
 
 #include "internal.h"
 #include "serve_common.cuh"
+#include "serve_host.h"
 
 namespace geon {
 cudaError_t launch_serve_fp64(int kind, const ServeJob* jobs, ServeCounters cnt, ServeClass* cl,
@@ -43,56 +44,13 @@ cudaError_t launch_serve_prologue(ServeClass* cls, int nclasses, unsigned* epoch
 }  // namespace geon
 
 using namespace geon;
+using namespace geon::serve_host;
 
 namespace {
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
-
-constexpr size_t ALIGN = 256;
-size_t rup(size_t n) { return (n + ALIGN - 1) & ~(ALIGN - 1); }
-
-// First-fit allocator over the device arena (host bookkeeping only).
-class Arena {
- public:
-  void init(size_t n) {
-    free_.clear();
-    free_[0] = n;
-  }
-  bool alloc(size_t n, size_t* off) {
-    n = rup(n ? n : 1);
-    for (auto it = free_.begin(); it != free_.end(); ++it) {
-      if (it->second >= n) {
-        const size_t o = it->first, rem = it->second - n;
-        free_.erase(it);
-        if (rem) free_[o + n] = rem;
-        *off = o;
-        return true;
-      }
-    }
-    return false;
-  }
-  void release(size_t off, size_t n) {
-    n = rup(n ? n : 1);
-    auto it = free_.emplace(off, n).first;
-    auto nx = std::next(it);
-    if (nx != free_.end() && it->first + it->second == nx->first) {
-      it->second += nx->second;
-      free_.erase(nx);
-    }
-    if (it != free_.begin()) {
-      auto pv = std::prev(it);
-      if (pv->first + pv->second == it->first) {
-        pv->second += it->second;
-        free_.erase(it);
-      }
-    }
-  }
-
- private:
-  std::map<size_t, size_t> free_;
-};
 
 // Carves consecutive 256-byte-aligned buffers out of a base pointer (or just
 // sums their sizes when base is null).
@@ -310,42 +268,17 @@ cudaError_t publish(geon_server* S, HostJob* J, const ServeJob& sj) {
 // rays, fewest unclaimed first (arrival order on ties), so a small request is
 // not queued behind a large one; rays already in flight continue first.
 void write_claim_order(geon_server* S) {
-  std::vector<std::pair<std::pair<int64_t, uint64_t>, int>> order[SERVE_CLASSES];
+  std::vector<ClaimEntry> entries;
   for (const HostJob* J : S->active) {
     if (!J->tracing || J->stop_flagged) continue;
     const int64_t claimed = (int64_t)S->h_counters[J->slot];
-    const int64_t left = J->nrays - (claimed < J->nrays ? claimed : J->nrays);
-    if (left > 0) order[J->cls].push_back({{left, J->id}, J->slot});
+    entries.push_back({J->cls, J->nrays - (claimed < J->nrays ? claimed : J->nrays), J->id, J->slot});
   }
+  unsigned counts[SERVE_CLASSES];
+  claim_order(entries, SERVE_CLASSES, SERVE_RING, S->h_order, counts);
   for (int c = 0; c < SERVE_CLASSES; ++c) {
-    std::sort(order[c].begin(), order[c].end());
-    int* dst = S->h_order + (size_t)c * SERVE_RING;
-    for (size_t i = 0; i < order[c].size(); ++i) dst[i] = order[c][i].second;
-    S->h_tail_head[2 * c] = (unsigned)order[c].size();
+    S->h_tail_head[2 * c] = counts[c];
     S->h_tail_head[2 * c + 1] = 0;
-  }
-}
-
-// Midpoints of the next `levels` halvings of [lo, hi] in heap order (node i at
-// index i-1, children 2i = [lo, mid] and 2i+1 = [mid, hi]), each 0.5*(lo+hi)
-// exactly as the sequential loop forms it.
-void bisect_tree(double lo, double hi, int levels, std::vector<double>& a) {
-  const int64_t per = ((int64_t)1 << levels) - 1;
-  a.assign(per, 0.0);
-  std::vector<double> nl(per), nh(per);
-  nl[0] = lo;
-  nh[0] = hi;
-  for (int64_t i = 1; i <= per; ++i) {
-    const double l = nl[i - 1], h = nh[i - 1], mid = 0.5 * (l + h);
-    a[i - 1] = mid;
-    if (2 * i <= per) {
-      nl[2 * i - 1] = l;
-      nh[2 * i - 1] = mid;
-    }
-    if (2 * i + 1 <= per) {
-      nl[2 * i] = mid;
-      nh[2 * i] = h;
-    }
   }
 }
 
