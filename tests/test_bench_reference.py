@@ -38,3 +38,13 @@ def test_curvature_cpu_leg(orc):
     for v in r.values():
         assert v["value"] > 0 and 256 <= v["points"] <= len(pts) and v["seconds"] > 0
     assert r["riemann_once"]["value"] > 3 * r["reference_call_graph"]["value"]
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    """Under torchrun (N > 1) rank 0 alone runs and prints the reference arm."""
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "3", "--cpu-rays", "16"], capture_output=True, text=True, timeout=600, cwd=ROOT,
+                         env=env)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert not [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
