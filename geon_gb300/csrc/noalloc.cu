@@ -10,16 +10,25 @@
 // "out of memory" halfway through a frame. For them this entry point keeps its
 // working memory in one fixed array compiled into the library instead.
 //
-// The array (NOALLOC_SCRATCH_BYTES, 512 KiB) is a __device__ variable: every GPU
-// that loads the library holds it until the process exits, whether or not the
-// entry point is ever called. It bounds the work: at most NOALLOC_MAX_BRACKETS
-// (4096) brackets per call; larger requests are refused with GEON_ERR_INVALID.
+// The array (NOALLOC_SCRATCH_BYTES, 512 KiB) is a __device__ variable: once it
+// is placed on a GPU it stays there until the process exits. It bounds the
+// work: at most NOALLOC_MAX_BRACKETS (4096) brackets per call; larger requests
+// are refused with GEON_ERR_INVALID. The speculative width of the bisection
+// rounds is always the default one (geon_set_bisect_rays_per_round does not
+// apply here): the array is sized for it.
 //
 // Host code cannot use the array's name as a device address (on the host it
-// names a stand-in object), so the first call on each device, with that device
-// current, asks the runtime for the array's device address with
-// cudaGetSymbolAddress and remembers it. Make that first call before capturing
-// any stream into a CUDA graph.
+// names a stand-in object), so every call, with the caller's device current,
+// asks the runtime for the array's device address with cudaGetSymbolAddress,
+// checks the result and hands that address to the kernels. The lookup is not
+// cached: a cached address would go stale when the context it came from is
+// destroyed (cudaDeviceReset) and another one takes its place. Under CUDA's
+// lazy module loading the array is only placed on a device when this lookup
+// first runs there, and the kernels' code when they first launch there, so the
+// first call on a device is the one that takes device memory (the array's
+// 512 KiB and the code): make it before the caller reserves the rest of the
+// device's memory for its own pool, and before capturing any stream into a
+// CUDA graph. Later calls find both loaded and take nothing.
 //
 // All calls share the one array and each leaves its contents behind; the entry
 // point clears what must start at zero. Two calls whose work overlaps on the
@@ -28,7 +37,6 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
-#include <mutex>
 
 #include "internal.h"
 
@@ -41,25 +49,14 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device (set up once per device).
+// Device address of the scratch array in the current context (looked up on
+// every call; the first lookup on a device loads the array there).
 int noalloc_scratch(unsigned char** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return set_last_error(GEON_ERR_CUDA, cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return set_last_error(GEON_ERR_INVALID, "device index out of range");
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return set_last_error(GEON_ERR_CUDA, e != cudaSuccess ? cudaGetErrorString(e) : "null scratch address");
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return set_last_error(GEON_ERR_CUDA, e != cudaSuccess ? cudaGetErrorString(e) : "null scratch address");
+  *out = static_cast<unsigned char*>(p);
   return GEON_OK;
 }
 
@@ -77,7 +74,8 @@ extern "C" int geon_shadow_bisect_dev_noalloc(geon_metric_t m, double r_obs, con
   const MetricDesc* d = metric_desc(m);
   if (!d) return set_last_error(GEON_ERR_INVALID, "null metric handle");
   if (d->kind != GEON_SCHWARZSCHILD) return set_last_error(GEON_ERR_INVALID, "shadow bisection needs a Schwarzschild metric");
-  if (precision != GEON_FP64 && precision != GEON_MIXED && precision != GEON_ADAPTIVE)
+  if (precision != GEON_FP64 && precision != GEON_MIXED && precision != GEON_ADAPTIVE &&
+      precision != GEON_FP64_FAST)
     return set_last_error(GEON_ERR_INVALID, "unknown precision");
   if (nb == 0) return GEON_OK;
   if (nb > NOALLOC_MAX_BRACKETS)
