@@ -1,24 +1,38 @@
-"""Benchmark: Schwarzschild shadow sweep + concurrent bisections (ray-steps/s).
+"""Benchmark: Schwarzschild shadow sweep + concurrent bisections (ray-steps/s),
+with the other workloads of the task measured beside it.
 
-Workload (one step), Schwarzschild M = 1 (horizon_pad 1.001, escape_radius 1000),
-observer r_obs = 20M, RK4 step 0.01, cap 200,000 steps (bin/validate_shadow.rs
-settings):
+Headline workload (one step), Schwarzschild M = 1 (horizon_pad 1.001,
+escape_radius 1000), observer r_obs = 20M, RK4 step 0.01, cap 200,000 steps
+(bin/validate_shadow.rs settings):
   * sweep: 2^20 equatorial rays with launch angle alpha ~ U[10 deg, 20 deg]
     (seeded), each classified captured / escaped;
   * 64 concurrent 40-iteration bisections of alpha_c from seeded brackets
     lo ~ U[13, 14] deg, hi ~ U[14.5, 15.5] deg.
 At r_obs = 20M the critical angle is 14.269 deg, inside both ranges (at 30M it
-would be 9.63 deg, outside them). Inputs are synthetic and seeded.
+is 9.63 deg, outside them; the 30M variant with its own ranges is a leg below).
+Inputs are synthetic and seeded.
 
 value = useful ray-steps (sweep steps + the bisections' sequential-path steps)
-per second of device time with inputs resident in HBM. The default precision
-is the mixed FP32/FP64 path; the plain FP64 path is timed beside it (one
-device-timed step over every 4th sweep ray and the bisections), and the accuracy of mixed vs FP64 is
-reported on a uniform 1/32 sample of the sweep.
-`--workload serve` runs the serving stream instead (serve_requests): a seeded
-Poisson stream of render, bisection and curvature requests through
-geon_gb300.Server (mixed; `--serve-precisions mixed,fp64` adds the FP64
-stream), with p50/p99 latency.
+per second of device time with inputs resident in HBM (mixed FP32/FP64 path).
+Beside it, in the same JSON line (rank 0, full workload):
+  accuracy      mixed vs FP64 classes on 1/32 of the sweep, traced with the
+                timed planar step, disagreements settled by the FP64 arbiter
+                (geon_gb300.accuracy); escape directions, null drift, b_c;
+  fp64_path     the plain FP64 path (the reference's arithmetic) on every 32nd
+                sweep ray + the 64 bisections, 5 device-timed steps: ray-steps/s
+                and p50/p99 step latency; fp64fast_path: GEON_FP64_FAST, 1 step;
+  e2e           the host API with pinned buffers, copies inside, repeated;
+  cpu_baseline  the C++ restatement of the reference on the host cores;
+  config1       256^2 Schwarzschild render (r 30M, fov 60, h 0.05, cap 20000):
+                FP64, FP64_FAST, mixed; the reference's own CUDA kernel at its
+                escape radius (1000M) beside FP64 and FP64_FAST there;
+  config3       2048^2 Alcubierre and Morris-Thorne renders (mixed, full
+                images) and their FP64 classes on a row sample;
+  config4       128^3 Alcubierre curvature grid (Einstein + 16 T(k, k)), FP64;
+  config2_r30   the sweep + bisections at r_obs = 30M (alpha ~ U[5, 15] deg,
+                brackets around 9.63 deg).
+`--workload serve|render|exotic|curvature` prints one of those as its own line
+(serve: the Poisson request stream through geon_gb300.Server).
 `--impl reference` times the CPU restatement of the reference (oracle/) on
 the host cores instead.
 """
@@ -29,6 +43,7 @@ import subprocess
 import sys
 import threading
 import time
+import traceback
 
 import numpy as np
 
@@ -51,7 +66,10 @@ SCHW = [1.0, 1.001, 1000.0]
 RESERVE = 5
 BISECT_RAYS = 16384  # speculative width of a bisection round (geon_set_bisect_rays_per_round)
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
+CURV_FLOPS_PER_POINT = 20000  # Alcubierre: 9 FD Christoffel evaluations, Riemann, contractions, 16 T(k, k)
 B_C = 3.0 * np.sqrt(3.0)
+# 30M variant: alpha_c = asin(3 sqrt(3) sqrt(1 - 2/30) / 30) = 9.633 deg
+R_OBS_30 = 30.0
 
 
 def workload(seed):
@@ -62,8 +80,22 @@ def workload(seed):
     return alpha, lo, hi
 
 
-def b_of(alpha):
-    return R_OBS * np.sin(alpha) / np.sqrt(1.0 - 2.0 / R_OBS)
+def workload_r30(seed):
+    rng = np.random.default_rng(seed)
+    alpha = np.radians(rng.uniform(5.0, 15.0, N_SWEEP))
+    lo = np.radians(rng.uniform(9.0, 9.5, N_BRACKETS))
+    hi = np.radians(rng.uniform(9.8, 10.3, N_BRACKETS))
+    return alpha, lo, hi
+
+
+def rank_workload(rank, seed=0x5EED):
+    """The headline workload of one rank: its own seeded sweep and brackets."""
+    from geon_gb300 import shard
+    return workload(shard.rank_seed(seed, rank))
+
+
+def b_of(alpha, r_obs=R_OBS):
+    return r_obs * np.sin(alpha) / np.sqrt(1.0 - 2.0 / r_obs)
 
 
 class ClockSampler:
@@ -120,11 +152,11 @@ class ClockSampler:
                 "power_w_max": max(power), "reasons": sorted(reasons)}
 
 
-def cpu_sample_rate(orc, alpha, n, threads):
+def cpu_sample_rate(orc, alpha, n, threads, r_obs=R_OBS):
     """Oracle (CPU restatement of the reference) on a uniform sample of the sweep."""
     sample = alpha[:: max(1, len(alpha) // n)][:n]
     t0 = time.perf_counter()
-    term, steps = orc.shadow_classify(SCHW, R_OBS, sample, STEP, MAX_STEPS, math=orc.LIBM, nthreads=threads)
+    term, steps = orc.shadow_classify(SCHW, r_obs, sample, STEP, MAX_STEPS, math=orc.LIBM, nthreads=threads)
     dt = time.perf_counter() - t0
     return float(steps.sum()) / dt, dt, int(steps.sum()), len(sample)
 
@@ -157,20 +189,91 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def pct(v, q):
+    return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if len(v) else None
+
+
+def leg(name, fn, *a, **kw):
+    """Run one measurement leg; an exception is reported in the line (and on
+    stderr) instead of losing the headline."""
+    t0 = time.perf_counter()
+    try:
+        out = fn(*a, **kw)
+    except Exception as e:  # noqa: BLE001 - reported, not hidden
+        traceback.print_exc()
+        out = {"error": f"{type(e).__name__}: {e}"}
+    print(f"[bench] leg {name}: {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
+    return out
+
+
+class SweepRunner:
+    """One step of the headline workload on the GPU: the sweep on stream sa
+    (persistent grid keeping `reserve` block slots per SM free) and the
+    bisections on stream sb, CUDA events on both."""
+
+    def __init__(self, lib, torch, h, args, dev):
+        self.lib, self.torch, self.h, self.args = lib, torch, h, args
+        self.sa, self.sb = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+        self.d_term = torch.empty(N_SWEEP, dtype=torch.int32, device=dev)
+        self.d_steps = torch.empty(N_SWEEP, dtype=torch.int64, device=dev)
+        self.d_ac = torch.empty(N_BRACKETS, dtype=torch.float64, device=dev)
+        self.d_bst = torch.empty(N_BRACKETS, dtype=torch.int64, device=dev)
+
+    def check(self, rc):
+        if rc != 0:
+            raise RuntimeError(self.lib.geon_last_error().decode())
+
+    def step(self, precision, alpha, lo, hi, r_obs=R_OBS, bisect=True, reserve=None):
+        torch, lib = self.torch, self.lib
+        n = alpha.numel()
+        main = torch.cuda.current_stream()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        ev[0].record(main)
+        self.sa.wait_stream(main)
+        self.sb.wait_stream(main)
+        ev[1].record(self.sa)
+        lib.geon_set_persistent_reserve_f(self.args.reserve if reserve is None else reserve)
+        self.check(lib.geon_shadow_classify_dev(self.h, r_obs, alpha.data_ptr(), n, STEP, MAX_STEPS, precision,
+                                                self.d_term.data_ptr(), self.d_steps.data_ptr(),
+                                                self.sa.cuda_stream))
+        lib.geon_set_persistent_reserve(0)
+        ev[2].record(self.sa)
+        ev[3].record(self.sb)
+        if bisect:
+            self.check(lib.geon_shadow_bisect_dev(self.h, r_obs, lo.data_ptr(), hi.data_ptr(), lo.numel(), ITERS,
+                                                  STEP, MAX_STEPS, precision, self.d_ac.data_ptr(), None, None,
+                                                  self.d_bst.data_ptr(), self.sb.cuda_stream))
+        ev[4].record(self.sb)
+        main.wait_stream(self.sa)
+        main.wait_stream(self.sb)
+        ev[5].record(main)
+        return ev
+
+    def result(self, ev, n, bisect=True):
+        self.torch.cuda.synchronize()
+        steps = int(self.d_steps[:n].sum().item()) + (int(self.d_bst.sum().item()) if bisect else 0)
+        return {"ms": ev[0].elapsed_time(ev[5]), "sweep_ms": ev[1].elapsed_time(ev[2]),
+                "bisection_ms": ev[3].elapsed_time(ev[4]), "steps": steps,
+                "sweep_steps": int(self.d_steps[:n].sum().item())}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp64fast"])
     ap.add_argument("--cpu-rays", type=int, default=4096)
     ap.add_argument("--bisect-rays", type=int, default=BISECT_RAYS,
                     help="speculative bisection width (rays per round over all brackets)")
     ap.add_argument("--reserve", type=float, default=RESERVE,
                     help="block slots per SM the sweep leaves free for the bisections (latency vs throughput)")
-    ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy leg traces every k-th sweep ray")
-    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 leg, accuracy, e2e and CPU legs")
+    ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy and FP64 legs trace every k-th sweep ray")
+    ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 latency leg")
+    ap.add_argument("--legs", default="all",
+                    help="comma list of legs beside the headline (accuracy,fp64,e2e,cpu,config1,config3,config4,"
+                         "r30), 'all' or 'none'")
     # small cases for profiling only (they change the workload; never a bench line)
     ap.add_argument("--rays", type=int, default=N_SWEEP, help="profiling: sweep size")
     ap.add_argument("--sweep-only", action="store_true", help="profiling: no bisections")
@@ -194,10 +297,9 @@ def main():
     import geon_gb300 as geon
     from geon_gb300 import _ffi, shard
     lib = _ffi.load()
-    prec = 1 if args.precision == "mixed" else 0
+    prec = {"fp64": 0, "mixed": 1, "fp64fast": 3}[args.precision]
     m = geon.Schwarzschild(SCHW[0], SCHW[1], args.escape_radius)
-    h = m.handle
-    alpha, lo, hi = workload(shard.rank_seed(0x5EED, rank))
+    alpha, lo, hi = rank_workload(rank)
     n_sweep = args.rays
     alpha = alpha[:n_sweep]
     dev = torch.device("cuda", local)
@@ -205,45 +307,10 @@ def main():
     d_alpha = torch.tensor(alpha, device=dev)
     d_lo = torch.tensor(lo, device=dev)
     d_hi = torch.tensor(hi, device=dev)
-    d_term = torch.empty(n_sweep, dtype=torch.int32, device=dev)
-    d_steps = torch.empty(n_sweep, dtype=torch.int64, device=dev)
-    d_ac = torch.empty(N_BRACKETS, dtype=torch.float64, device=dev)
-    d_bst = torch.empty(N_BRACKETS, dtype=torch.int64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
-    sa, sb = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
-
-    def check(rc):
-        if rc != 0:
-            raise RuntimeError(lib.geon_last_error().decode())
-
+    run = SweepRunner(lib, torch, m.handle, args, dev)
     lib.geon_set_bisect_rays_per_round(args.bisect_rays)
-
-    def one_step(precision, sweep=None):
-        s_alpha, s_n = sweep if sweep is not None else (d_alpha, n_sweep)
-        main = torch.cuda.current_stream()
-        e0 = torch.cuda.Event(enable_timing=True)
-        ea0, ea1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        eb0, eb1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(main)
-        sa.wait_stream(main)
-        sb.wait_stream(main)
-        ea0.record(sa)
-        lib.geon_set_persistent_reserve_f(args.reserve)  # leave room on every SM for the bisection rounds
-        check(lib.geon_shadow_classify_dev(h, R_OBS, s_alpha.data_ptr(), s_n, STEP, MAX_STEPS, precision,
-                                           d_term.data_ptr(), d_steps.data_ptr(), sa.cuda_stream))
-        lib.geon_set_persistent_reserve(0)
-        ea1.record(sa)
-        eb0.record(sb)
-        if not args.sweep_only:
-            check(lib.geon_shadow_bisect_dev(h, R_OBS, d_lo.data_ptr(), d_hi.data_ptr(), N_BRACKETS, ITERS, STEP,
-                                             MAX_STEPS, precision, d_ac.data_ptr(), None, None, d_bst.data_ptr(),
-                                             sb.cuda_stream))
-        eb1.record(sb)
-        main.wait_stream(sa)
-        main.wait_stream(sb)
-        e1.record(main)
-        return e0, e1, ea0, ea1, eb0, eb1
+    bis = not args.sweep_only
 
     def barrier():
         torch.cuda.synchronize()
@@ -252,79 +319,79 @@ def main():
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
-        one_step(prec)
+        run.result(run.step(prec, d_alpha, d_lo, d_hi, bisect=bis), n_sweep, bis)
         flush.zero_()
     barrier()
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = lib.geon_launch_count()
-    times, sweep_ms, bis_ms, total_steps = [], [], [], 0
+    res = []
     barrier()
     for _ in range(args.steps):
-        ev = one_step(prec)
-        torch.cuda.synchronize()
-        times.append(ev[0].elapsed_time(ev[1]))
-        sweep_ms.append(ev[2].elapsed_time(ev[3]))
-        bis_ms.append(ev[4].elapsed_time(ev[5]))
-        total_steps += int(d_steps.sum().item()) + (0 if args.sweep_only else int(d_bst.sum().item()))
+        ev = run.step(prec, d_alpha, d_lo, d_hi, bisect=bis)
+        res.append(run.result(ev, n_sweep, bis))
         flush.zero_()  # between timed iterations, outside the events
     barrier()
     launches = lib.geon_launch_count() - launches0
     clocks = sampler.stop()
-    t_total, total_steps = shard.job_totals(dist, sum(times) / 1e3, total_steps, dev)
+    times = [r["ms"] for r in res]
+    t_total, total_steps = shard.job_totals(dist, sum(times) / 1e3, sum(r["steps"] for r in res), dev)
     value = total_steps / t_total
-    sweep_steps = int(d_steps.sum().item())
-    sweep_term = d_term.cpu().numpy()
-    ac_mixed = d_ac.cpu().numpy()
-    fp64_leg = None
-    full = n_sweep == N_SWEEP and not args.sweep_only and args.escape_radius == SCHW[2]
-    if prec == 1 and full and not args.no_extras:
-        # The plain FP64 path, device-timed on the same kind of step: every 4th
-        # sweep ray (262144 rays, over 3 rays per resident FP64 lane) plus all
-        # 64 bisections. (GB300 runs FP64 at 1/62 of its FP32 rate; the full
-        # sweep would take minutes.)
-        sub = d_alpha[::4].contiguous()
-        flush.zero_()
-        torch.cuda.synchronize()
-        ev = one_step(0, (sub, sub.numel()))
-        torch.cuda.synchronize()
-        ms64 = ev[0].elapsed_time(ev[1])
-        steps64 = int(d_steps[:sub.numel()].sum().item()) + int(d_bst.sum().item())
-        fp64_leg = {"value": steps64 / (ms64 / 1e3), "unit": "ray-steps/s", "ms_per_step": ms64,
-                    "sweep_ms": ev[2].elapsed_time(ev[3]), "bisection_ms": ev[4].elapsed_time(ev[5]),
-                    "sample": "every 4th sweep ray + the 64 bisections, one step, CUDA events",
-                    "mixed_over_fp64": value / (steps64 / (ms64 / 1e3))}
+    sweep_steps = res[-1]["sweep_steps"]
+    ac_run = run.d_ac.cpu().numpy()
+    full = n_sweep == N_SWEEP and bis and args.escape_radius == SCHW[2]
+    legs = set() if args.legs == "none" or not full else (
+        {"accuracy", "fp64", "e2e", "cpu", "config1", "config3", "config4", "r30"} if args.legs == "all"
+        else set(args.legs.split(",")))
+    extras = {}
+    # the plain FP64 path on the same kind of step (every rank: a shard of the job)
+    if prec == 1 and "fp64" in legs:
+        extras["fp64_path"] = leg("fp64_path", fp64_latency_leg, run, torch, flush, d_alpha, d_lo, d_hi, args,
+                                  value, 0, args.fp64_steps)
+        extras["fp64fast_path"] = leg("fp64fast_path", fp64_latency_leg, run, torch, flush, d_alpha, d_lo, d_hi,
+                                      args, value, 3, 1)
 
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return
 
-    extras = {}
     peak32 = ctypes_peak(lib, 0)
     peak64 = ctypes_peak(lib, 1)
-    kernel_s = float(np.mean(sweep_ms)) / 1e3
+    kernel_s = float(np.mean([r["sweep_ms"] for r in res])) / 1e3
     achieved = ALG_FLOPS_PER_STEP * sweep_steps / kernel_s / 1e12
     peak = peak32 if prec == 1 else peak64
-    traffic = load_traffic()
     roofline = {"bound": "fp32 pipe" if prec == 1 else "fp64 pipe", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": load_traffic(),
                 "kernel": "trace_mixed_kernel<Schwarzschild, equatorial, shadow>" if prec == 1 else
                 "trace_fp64_kernel<Schwarzschild, equatorial, shadow>",
                 "alg_flops_per_ray_step": ALG_FLOPS_PER_STEP,
                 "peak_source": "measured in this run: FFMA/DFMA throughput probe (geon_probe_fma_peak); "
-                               "MEASURED_PEAKS.json has no FP32/FP64 non-tensor peak"}
-
-    if not args.no_extras and full:
-        extras = extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_mixed, prec, dev, value)
-    if fp64_leg is not None:
-        extras["fp64_path"] = fp64_leg
+                               "MEASURED_PEAKS.json has no FP32/FP64 non-tensor peak",
+                "peaks_measured": {"fp32_tflops": peak32, "fp64_tflops": peak64}}
+    if "accuracy" in legs:
+        extras["accuracy"] = leg("accuracy", accuracy_leg, geon, m, alpha, lo, hi, ac_run, args.fp64_sample)
+    if "e2e" in legs:
+        extras["e2e"] = leg("e2e", e2e_leg, geon, m, alpha, lo, hi, args.precision, min(args.steps, 10))
+    if "cpu" in legs:
+        extras["cpu_baseline"] = leg("cpu", cpu_leg, alpha, args.cpu_rays)
+    if "config1" in legs:
+        extras["config1"] = leg("config1", config1_leg, geon, lib, peak64)
+    if "config3" in legs:
+        extras["config3"] = leg("config3", config3_leg, geon, lib, 2048, 64)
+    if "config4" in legs:
+        extras["config4"] = leg("config4", config4_leg, geon, 128, peak64)
+    if "r30" in legs:
+        extras["config2_r30"] = leg("r30", r30_leg, geon, lib, run, torch, flush, dev, prec)
+    if "fp64_path" in extras and "ray_steps_per_s" in extras["fp64_path"]:
+        extras["mixed_over_fp64"] = value / extras["fp64_path"]["ray_steps_per_s"]
 
     line = {
         "metric": "ray-steps/s", "value": value, "unit": "ray-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (mixed: FP32 right-hand side, compensated f32-pair state)" if prec == 1 else "f64",
+        "dtype": {1: "f32 (mixed: FP32 right-hand side, compensated f32-pair state)", 0: "f64",
+                  3: "f64 (fast: fused, reassociated)"}[prec],
         "data": "synthetic (seeded alpha and brackets)",
         "config": {"workload": "schwarzschild shadow sweep: 2^20 equatorial rays alpha~U[10,20] deg + 64 concurrent "
                                "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
@@ -333,18 +400,399 @@ def main():
                    "sweep_reserve_blocks_per_sm": args.reserve, "bisect_rays_per_round": args.bisect_rays,
                    "mixed_kernel_variant": None if tuned is None else tuned["variant"][1],
                    "autotune_rates": None if tuned is None else tuned.get("rates")},
-        "latency": {"bisection_ms_p50": float(np.percentile(bis_ms, 50)),
-                    "bisection_ms_p99": float(np.percentile(bis_ms, 99)),
-                    "sweep_ms_p50": float(np.percentile(sweep_ms, 50)),
-                    "sweep_ms_p99": float(np.percentile(sweep_ms, 99))},
+        "latency": {"step_ms_p50": pct(times, 50), "step_ms_p99": pct(times, 99),
+                    "bisection_ms_p50": pct([r["bisection_ms"] for r in res], 50),
+                    "bisection_ms_p99": pct([r["bisection_ms"] for r in res], 99),
+                    "sweep_ms_p50": pct([r["sweep_ms"] for r in res], 50),
+                    "sweep_ms_p99": pct([r["sweep_ms"] for r in res], 99)},
         "roofline": roofline,
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if "fp64_path" in extras and "latency" in extras["fp64_path"]:
+        line["latency"]["fp64"] = extras["fp64_path"]["latency"]
     line.update(extras)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def fp64_latency_leg(run, torch, flush, d_alpha, d_lo, d_hi, args, value, precision, steps):
+    """An FP64 precision on the headline's kind of step: every fp64_sample-th
+    sweep ray (the whole sweep would take minutes: GB300 runs FP64 at 1/62 of
+    its FP32 rate) beside all 64 bisections, `steps` device-timed steps."""
+    sub = d_alpha[:: max(1, args.fp64_sample)].contiguous()
+    out = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        out.append(run.result(run.step(precision, sub, d_lo, d_hi), sub.numel()))
+    ms = [o["ms"] for o in out]
+    rate = sum(o["steps"] for o in out) / (sum(ms) / 1e3)
+    return {"ray_steps_per_s": rate, "unit": "ray-steps/s", "steps": steps, "sweep_rays": int(sub.numel()),
+            "latency": {"step_ms_p50": pct(ms, 50), "step_ms_p99": pct(ms, 99),
+                        "bisection_ms_p50": pct([o["bisection_ms"] for o in out], 50),
+                        "bisection_ms_p99": pct([o["bisection_ms"] for o in out], 99),
+                        "sweep_ms_p50": pct([o["sweep_ms"] for o in out], 50),
+                        "sweep_ms_p99": pct([o["sweep_ms"] for o in out], 99)},
+            "sample": f"every {args.fp64_sample}th sweep ray + the 64 bisections per step, CUDA events",
+            "mixed_over_this": value / rate}
+
+
+def accuracy_leg(geon, m, alpha, lo, hi, ac_run, k):
+    """Mixed vs FP64 on a uniform 1/k sample of the sweep, both traced by the
+    equatorial entry point with the steppers the sweep uses (the mixed path's
+    planar step)."""
+    sample = alpha[::k]
+    r64 = geon.shadow.trace(m, R_OBS, sample, STEP, MAX_STEPS, precision="fp64")
+    rmx = geon.shadow.trace(m, R_OBS, sample, STEP, MAX_STEPS, precision="mixed")
+    y0 = geon.shadow.equatorial_ray(m, R_OBS, sample)
+    rep = geon.accuracy.class_report(m, y0, STEP, MAX_STEPS, rmx.termination, r64.termination)
+    esc = geon.accuracy.clean_escapes(m, r64) & geon.accuracy.clean_escapes(m, rmx)
+    d64 = m.asymptotic_direction(r64.final_state[esc])
+    dmx = m.asymptotic_direction(rmx.final_state[esc])
+    ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0))
+    ac64, _, _, _ = geon.shadow.bisect(m, R_OBS, lo, hi, ITERS, STEP, MAX_STEPS, precision="fp64")
+    acm, _, _, _ = geon.shadow.bisect(m, R_OBS, lo, hi, ITERS, STEP, MAX_STEPS, precision="mixed")
+    vs_m, _, _, _ = geon.shadow.bisect(m, R_OBS, 0.0, np.pi / 2 - 1e-3, 60, STEP, MAX_STEPS, precision="mixed")
+    rel64 = np.abs(b_of(ac64) - B_C) / B_C
+    relm = np.abs(b_of(acm) - B_C) / B_C
+    return {
+        "sample_rays": int(len(sample)),
+        "stepper": "the timed planar equatorial step (geon_shadow_trace)",
+        "classes_vs_fp64": rep,
+        "class_mismatch_vs_fp64_raw": rep["raw_mismatch"],
+        "class_mismatch_vs_arbiter": rep["mismatch_vs_arbiter"],
+        "escape_dir_angle_err_rad_max": float(ang.max()) if ang.size else None,
+        "escape_dir_angle_err_rad_p50": float(np.median(ang)) if ang.size else None,
+        "escape_dir_angle_err_rad_p99": float(np.quantile(ang, 0.99)) if ang.size else None,
+        "null_drift_max_escaped_mixed": float(np.max(rmx.null_residual[esc])) if esc.any() else None,
+        "null_drift_max_escaped_fp64": float(np.max(r64.null_residual[esc])) if esc.any() else None,
+        "escapes_compared": int(esc.sum()),
+        "b_c_validate_shadow_bracket_mixed_rel_err": float(abs(b_of(vs_m[0]) - B_C) / B_C),
+        "b_c_brackets_within_1e-6_mixed": int(np.sum(relm <= 1e-6)),
+        "b_c_brackets_within_1e-6_fp64": int(np.sum(rel64 <= 1e-6)),
+        "b_c_rel_err_mixed_p50": float(np.median(relm)),
+        "b_c_rel_err_mixed_max": float(relm.max()),
+        "b_c_rel_err_fp64_p50": float(np.median(rel64)),
+        "b_c_rel_err_fp64_max": float(rel64.max()),
+        "b_c_this_run_rel_err_max": float(np.max(np.abs(b_of(ac_run) - B_C) / B_C)),
+    }
+
+
+def e2e_leg(geon, m, alpha, lo, hi, prec_name, reps):
+    """The public host API with pinned host buffers (copies inside the timed
+    region): sweep and bisections on two host threads, `reps` timed steps
+    after one warm-up."""
+    import torch
+    pa = torch.tensor(alpha).pin_memory().numpy()
+    plo = torch.tensor(lo).pin_memory().numpy()
+    phi = torch.tensor(hi).pin_memory().numpy()
+    res = {}
+
+    def sweep():
+        res["sweep"] = geon.shadow.classify(m, R_OBS, pa, STEP, MAX_STEPS, precision=prec_name)
+
+    def bis():
+        res["bis"] = geon.shadow.bisect(m, R_OBS, plo, phi, ITERS, STEP, MAX_STEPS, precision=prec_name)
+
+    times, steps = [], []
+    for i in range(reps + 1):
+        t0 = time.perf_counter()
+        th = threading.Thread(target=bis)
+        th.start()
+        sweep()
+        th.join()
+        dt = time.perf_counter() - t0
+        if i > 0:
+            times.append(dt)
+            steps.append(int(res["sweep"][1].sum()) + int(res["bis"][3].sum()))
+    return {"value": float(sum(steps) / sum(times)), "unit": "ray-steps/s",
+            "h2d_bytes_per_step": N_SWEEP * 8 + 2 * N_BRACKETS * 8,
+            "d2h_bytes_per_step": N_SWEEP * (4 + 8) + N_BRACKETS * (8 * 3 + 8),
+            "steps": reps, "ms_p50": 1e3 * pct(times, 50), "ms_p99": 1e3 * pct(times, 99),
+            "ms_min": 1e3 * min(times), "ms_max": 1e3 * max(times),
+            "api": "geon_shadow_classify + geon_shadow_bisect (host pointers, two threads)"}
+
+
+def cpu_leg(alpha, n):
+    from oracle import oracle as orc
+    threads = orc.hardware_threads()
+    rate, dt, st, ns = cpu_sample_rate(orc, alpha, n, threads)
+    return {"value": rate, "unit": "ray-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{ns} rays uniform over the sweep ({st} ray-steps, {dt:.1f} s)"}
+
+
+def _wall(fn, reps):
+    """Best-of-reps wall time of fn() (host API calls return with results on the host)."""
+    best, out = 1e30, None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = fn()
+        best = min(best, time.perf_counter() - t0)
+    return best, out
+
+
+def _kernel_trace_ms(geon, m, y0, step, max_steps, precision, reps=2):
+    """Device time of geon_trace_dev (the trace kernel alone: states resident in
+    HBM, CUDA events on the launching stream); returns (ms, total steps)."""
+    import torch
+    n = len(y0)
+    dy0 = torch.tensor(np.ascontiguousarray(y0), device="cuda")
+    term = torch.empty(n, dtype=torch.int32, device="cuda")
+    yf = torch.empty((n, 8), dtype=torch.float64, device="cuda")
+    st = torch.empty(n, dtype=torch.int64, device="cuda")
+    rs = torch.empty(n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    ms = []
+    for i in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        geon.trace_dev(m, n, dy0.data_ptr(), step, max_steps, term.data_ptr(), yf.data_ptr(), st.data_ptr(),
+                       rs.data_ptr(), stream=s.cuda_stream, precision=precision)
+        e1.record(s)
+        torch.cuda.synchronize()
+        if i > 0:
+            ms.append(e0.elapsed_time(e1))
+    return min(ms), int(st.sum().item())
+
+
+def config1_leg(geon, lib, peak64):
+    """BASELINE config 1: Schwarzschild 256^2, observer r 30M, fov 60, h 0.05,
+    cap 20000, escape 100M, stars on; and the reference's CUDA kernel at its
+    own escape radius (1000M) beside the FP64 paths there."""
+    from oracle import oracle as orc
+    obs = [0.0, 30.0, np.pi / 2, 0.0]
+    cam = geon.Camera(obs, 60.0, 256, 256)
+    m = geon.Schwarzschild(1.0, 1.001, 100.0)
+    out = {"workload": "schwarzschild render 256x256, r_obs 30M, fov 60, h 0.05, cap 20000, escape 100M, stars on"}
+    res = {}
+    for prec in ("fp64", "fp64fast", "mixed"):
+        cfg = geon.RenderConfig(precision=prec, show_stars=True)
+        geon.render(m, cam, cfg)
+        dt, (rgb, st, cls, pst) = _wall(lambda: geon.render(m, cam, cfg, with_classes=True), 3)
+        res[prec] = {"ray_steps_per_s": st.total_steps / dt, "ms": 1e3 * dt, "total_steps": st.total_steps,
+                     "captured": st.captured, "escaped": st.escaped, "diverged": st.diverged, "cls": cls.ravel()}
+    y0 = cam.ray_states(cam.tetrad(m))
+    for prec in ("fp64fast", "mixed"):
+        res[prec]["classes_vs_fp64"] = geon.accuracy.class_report(m, y0, 0.05, 20000, res[prec]["cls"],
+                                                                 res["fp64"]["cls"])
+    # the FP64 path against the oracle (the reference's algorithm) on a row sample
+    rows = np.arange(0, 256, 16)
+    threads = orc.hardware_threads()
+    ys = y0.reshape(256, 256, 8)[rows].reshape(-1, 8)
+    t0 = time.perf_counter()
+    oterm, _, osteps, _ = orc.trace(1, [1.0, 1.001, 100.0], ys, 0.05, 20000, math=orc.LIBM, nthreads=threads)
+    dt_cpu = time.perf_counter() - t0
+    out["fp64_classes_equal_libm_oracle_rows"] = float(np.mean(res["fp64"]["cls"].reshape(256, 256)[rows].ravel()
+                                                               == oterm))
+    for r in res.values():
+        r.pop("cls")
+    out["render"] = res
+    # kernel-only FP64_FAST time, for its roofline (FP64 pipe)
+    kms, ksteps = _kernel_trace_ms(geon, m, y0, 0.05, 20000, "fp64fast")
+    ach = ALG_FLOPS_PER_STEP * ksteps / (kms / 1e3) / 1e12
+    out["roofline_fp64fast"] = {"bound": "fp64 pipe", "achieved": ach, "peak": peak64, "unit": "TFLOP/s",
+                                "frac": ach / peak64 if peak64 else None, "kernel_ms": kms,
+                                "kernel": "trace_fp64fast_kernel<array, trace>",
+                                "alg_flops_per_ray_step": ALG_FLOPS_PER_STEP}
+    kms64, ksteps64 = _kernel_trace_ms(geon, m, y0, 0.05, 20000, "fp64")
+    ach64 = ALG_FLOPS_PER_STEP * ksteps64 / (kms64 / 1e3) / 1e12
+    out["roofline_fp64"] = {"bound": "fp64 pipe", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
+                            "frac": ach64 / peak64 if peak64 else None, "kernel_ms": kms64,
+                            "kernel": "trace_fp64_kernel<Schwarzschild, array, trace>"}
+    # at the reference CUDA program's escape radius (1000M)
+    m1000 = geon.Schwarzschild(1.0, 1.001, 1000.0)
+    at1000 = {}
+    for prec in ("fp64", "fp64fast"):
+        cfg = geon.RenderConfig(precision=prec, show_stars=True)
+        geon.render(m1000, cam, cfg)
+        dt, (_, st) = _wall(lambda: geon.render(m1000, cam, cfg), 2)
+        at1000[prec] = {"ms": 1e3 * dt, "total_steps": st.total_steps, "ray_steps_per_s": st.total_steps / dt,
+                        "captured": st.captured, "escaped": st.escaped, "diverged": st.diverged}
+    ref = reference_gpu_bar(256, 256, 30.0, 60.0, 0.05, 20000, reps=2)
+    at1000["reference_cuda_kernel"] = ref
+    if "ms" in ref:
+        at1000["fp64fast_speedup_over_reference_kernel"] = ref["ms"] / at1000["fp64fast"]["ms"]
+        at1000["fp64_speedup_over_reference_kernel"] = ref["ms"] / at1000["fp64"]["ms"]
+    at1000["note"] = ("the reference CUDA program's settings: 256x256 r 30 fov 60 h 0.05 cap 20000, escape fixed at "
+                      "1000M; ours through the host render API (wall time, copies included), the reference kernel "
+                      "wall time around launch + sync")
+    out["escape_1000M"] = at1000
+    out["cpu_baseline"] = {"value": float(osteps.sum()) / dt_cpu, "unit": "ray-steps/s", "cores": threads,
+                           "kind": "port", "sample": f"every 16th row ({len(ys)} rays, {dt_cpu:.1f} s)"}
+    return out
+
+
+def config3_leg(geon, lib, n, row_step):
+    """BASELINE config 3: 2048^2 Alcubierre (R 2, thickness 0.125, v 0.5,
+    observer x = -10 looking +x) and Morris-Thorne (b0 1, observer l = 10)
+    renders, fov 90, h 0.05, cap 20000: mixed on the full images; FP64 (the
+    reference's FD-fallback Christoffel symbols) on every row_step-th row; the
+    oracle on one row."""
+    from oracle import oracle as orc
+    cases = {"alcubierre": (geon.Alcubierre(2.0, 0.125, 0.5, 0.0), 2, [2.0, 0.125, 0.5, 0.0],
+                            [0.0, -10.0, 0.0, 0.0], -1),
+             "morris_thorne": (geon.MorrisThorne(1.0), 3, [1.0], [0.0, 10.0, np.pi / 2, 0.0], 1)}
+    out = {"workload": f"exotic renders {n}x{n}: alcubierre (R 2, thickness 0.125, v 0.5) and morris-thorne (b0 1), "
+                       "fov 90, h 0.05, cap 20000"}
+    threads = orc.hardware_threads()
+    for name, (m, kind, params, obs, fwd) in cases.items():
+        geon.autotune.autotune(m)
+        cam = geon.Camera(obs, 90.0, n, n, forward_sign=fwd)
+        cfg = geon.RenderConfig(precision="mixed", show_stars=True)
+        geon.render(m, geon.Camera(obs, 90.0, 64, 64, forward_sign=fwd), cfg)
+        dt, (_, st) = _wall(lambda: geon.render(m, cam, cfg), 1)
+        rows = np.arange(0, n, row_step)
+        y0 = cam.ray_states(cam.tetrad(m)).reshape(n, n, 8)[rows].reshape(-1, 8)
+        t0 = time.perf_counter()
+        r64 = geon.trace(m, y0, 0.05, 20000, precision="fp64")
+        dt64 = time.perf_counter() - t0
+        rmx = geon.trace(m, y0, 0.05, 20000, precision="mixed")
+        rep = geon.accuracy.class_report(m, y0, 0.05, 20000, rmx.termination, r64.termination)
+        esc = geon.accuracy.clean_escapes(m, r64) & geon.accuracy.clean_escapes(m, rmx)
+        d64 = m.asymptotic_direction(r64.final_state[esc])
+        dmx = m.asymptotic_direction(rmx.final_state[esc])
+        ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0)) if esc.any() else np.zeros(1)
+        yc = y0[:n]  # the first sampled row
+        t0 = time.perf_counter()
+        _, _, osteps, _ = orc.trace(kind, params, yc, 0.05, 20000, math=orc.LIBM, nthreads=threads)
+        dt_cpu = time.perf_counter() - t0
+        out[name] = {"mixed_ray_steps_per_s": st.total_steps / dt, "mixed_ms": 1e3 * dt,
+                     "mixed_total_steps": st.total_steps,
+                     "fp64_ray_steps_per_s": float(r64.steps_taken.sum()) / dt64,
+                     "fp64_sample": f"every {row_step}th row ({len(y0)} rays), host API wall time",
+                     "mixed_over_fp64": (st.total_steps / dt) / (float(r64.steps_taken.sum()) / dt64),
+                     "classes_vs_fp64": rep,
+                     "escape_dir_err_rad_p50": float(np.median(ang)), "escape_dir_err_rad_p99":
+                         float(np.quantile(ang, 0.99)), "escape_dir_err_rad_max": float(ang.max()),
+                     "cpu_baseline": {"value": float(osteps.sum()) / dt_cpu, "unit": "ray-steps/s", "cores": threads,
+                                      "kind": "port", "sample": f"row 0 ({len(yc)} rays, {dt_cpu:.1f} s)"}}
+    out["mixed_ray_steps_per_s_both"] = (sum(out[c]["mixed_total_steps"] for c in cases)
+                                         / sum(out[c]["mixed_ms"] / 1e3 for c in cases))
+    return out
+
+
+def curvature_cpu_leg(orc, params, pts, threads, budget_s=3.0):
+    """The config-4 job per grid point (Einstein tensor + T(k, k) for 16 null
+    vectors) on the oracle, on a uniform sample of the grid sized to about
+    budget_s each: once with the reference's call graph (Riemann formed again
+    inside every curvature.rs call: twice for the Einstein tensor, twice per
+    vector for T(k, k)) and once with Riemann formed once per point (the same
+    bits). The cost does not depend on the vectors' values, so 16 copies of the
+    reference's own k = (1, 1, 0, 0) stand in for them."""
+    k = np.tile([[1.0, 1.0, 0.0, 0.0]], (16, 1))
+    out = {}
+    for name, faithful in (("reference_call_graph", True), ("riemann_once", False)):
+        def run(m):
+            sub = pts[np.linspace(0, len(pts) - 1, m).astype(np.int64)]
+            t0 = time.perf_counter()
+            orc.curvature(2, params, sub, "einstein", math=orc.LIBM, faithful=faithful, nthreads=threads)
+            orc.nec(2, params, sub, k, math=orc.LIBM, faithful=faithful, nthreads=threads)
+            return time.perf_counter() - t0
+        m = min(len(pts), 256)
+        dt = run(m)
+        m = int(min(len(pts), max(m, m * budget_s / max(dt, 1e-6))))
+        dt = run(m)
+        out[name] = {"value": m / dt, "points": m, "seconds": dt}
+    return out
+
+
+def config4_leg(geon, n, peak64, cpu_budget_s=3.0):
+    """BASELINE config 4 (FP64): 128^3 Alcubierre (v_s 0.5, R 2, sigma 8) grid,
+    Einstein + T(k, k) for 16 null vectors per point; a 4096-point
+    Morris-Thorne line; 1e5 Schwarzschild vacuum points (Ricci scalar)."""
+    import torch
+    from oracle import oracle as orc
+    threads = orc.hardware_threads()
+    alc = geon.Alcubierre(2.0, 0.125, 0.5, 0.0)
+    lo, hi = (-4.0, -4.0, -4.0), (4.0, 4.0, 4.0)
+    geon.curvature.grid(alc, lo, hi, (8, 8, 8), nk=16)
+    dt, (pts, ein, nec, _) = _wall(lambda: geon.curvature.grid(alc, lo, hi, (n, n, n), nk=16), 1)
+    sub = np.arange(0, len(pts), max(1, len(pts) // 1024))
+    oein = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.GEON, nthreads=threads)
+    bit_exact = bool(np.array_equal(oein.reshape(-1, 16), ein[sub].reshape(-1, 16)))
+    oein_libm = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.LIBM, nthreads=threads)
+    bit_exact_libm = bool(np.array_equal(oein_libm.reshape(-1, 16), ein[sub].reshape(-1, 16)))
+    cpu = curvature_cpu_leg(orc, [2.0, 0.125, 0.5, 0.0], pts, threads, cpu_budget_s)
+    st = torch.cuda.current_stream()
+    ein_d = torch.empty(len(pts) * 16, dtype=torch.float64, device="cuda")
+    nec_d = torch.empty(len(pts) * 16, dtype=torch.float64, device="cuda")
+    launch = lambda: geon.curvature.grid_dev(alc, lo, hi, (n, n, n), ein_d, nec_d, nk=16,  # noqa: E731
+                                             stream=st.cuda_stream)
+    for _ in range(3):
+        launch()
+    reps = 5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        launch()  # each launch writes 537 MB of results: more than L2 between launches
+    e1.record(st)
+    torch.cuda.synchronize()
+    kernel_ms = e0.elapsed_time(e1) / reps
+    dev_same = bool(np.array_equal(ein_d.cpu().numpy().reshape(-1, 16), ein.reshape(-1, 16))
+                    and np.array_equal(nec_d.cpu().numpy().reshape(-1, 16), nec.reshape(-1, 16)))
+    del ein_d, nec_d
+    ach = CURV_FLOPS_PER_POINT * len(pts) / (kernel_ms / 1e3) / 1e12
+    mt = geon.MorrisThorne(1.0)
+    dt_mt, (mpts, mein, mnec, _) = _wall(lambda: geon.curvature.grid(mt, (-5, np.pi / 2, 0), (5, np.pi / 2, 0),
+                                                                     (4096, 1, 1), nk=16), 2)
+    i0 = int(np.argmin(np.abs(mpts[:, 1])))
+    g = mt.g(mpts[i0])
+    T = geon.curvature.stress_energy(mt, mpts[i0])
+    ttt_mixed = float(np.linalg.inv(g)[0, 0] * T[0, 0])  # T^t_t at the point nearest the throat
+    rng = np.random.default_rng(7)
+    x = np.stack([np.zeros(100000), rng.uniform(3.0, 50.0, 100000), rng.uniform(0.1, np.pi - 0.1, 100000),
+                  rng.uniform(0.0, 2 * np.pi, 100000)], axis=1)
+    sch = geon.Schwarzschild(1.0)
+    dt_s, rs = _wall(lambda: geon.curvature.ricci_scalar(sch, x), 2)
+    return {"workload": f"curvature grid {n}^3 alcubierre (v_s 0.5, R 2, sigma 8) einstein + 16 null T(k,k) per point",
+            "points_per_s": len(pts) / dt, "host_api_ms": 1e3 * dt, "kernel_ms": kernel_ms,
+            "kernel_points_per_s": len(pts) / (1e-3 * kernel_ms),
+            "roofline": {"bound": "fp64 pipe", "achieved": ach, "peak": peak64, "unit": "TFLOP/s",
+                         "frac": ach / peak64 if peak64 else None, "kernel": "curvature_grid_kernel<Alcubierre>",
+                         "alg_flops_per_point": CURV_FLOPS_PER_POINT,
+                         "hbm_gbs": len(pts) * (16 + 16) * 8 / (kernel_ms / 1e3) / 1e9},
+            "device_api_same_bits": dev_same, "bit_exact_vs_oracle_geon_sample": bit_exact,
+            "bit_exact_vs_oracle_libm_sample": bit_exact_libm,
+            "morris_thorne_line": {"points": 4096, "ms": 1e3 * dt_mt, "points_per_s": 4096 / dt_mt,
+                                   "T_t_t_nearest_throat": ttt_mixed, "l_nearest_throat": float(mpts[i0, 1]),
+                                   "minus_1_over_8pi": -1.0 / (8.0 * np.pi)},
+            "schwarzschild_vacuum": {"points": 100000, "ms": 1e3 * dt_s, "points_per_s": 1e5 / dt_s,
+                                     "max_abs_ricci_scalar": float(np.max(np.abs(rs)))},
+            "cpu_baseline": {"value": cpu["reference_call_graph"]["value"], "unit": "grid-points/s",
+                             "cores": threads, "kind": "port",
+                             "sample": (f"{cpu['reference_call_graph']['points']} grid points, Einstein + 16 T(k,k) "
+                                        f"each, curvature.rs call graph ({cpu['reference_call_graph']['seconds']:.1f}"
+                                        " s)"),
+                             "riemann_once": cpu["riemann_once"]}}
+
+
+def r30_leg(geon, lib, run, torch, flush, dev, prec):
+    """The headline workload at r_obs = 30M (alpha ~ U[5, 15] deg, brackets
+    lo ~ U[9, 9.5], hi ~ U[9.8, 10.3] deg around alpha_c = 9.633 deg): one
+    device-timed step, and its accuracy on 1/64 of the sweep."""
+    alpha, lo, hi = workload_r30(0x5EED + 30)
+    m = geon.Schwarzschild(SCHW[0], SCHW[1], SCHW[2])
+    da, dlo, dhi = (torch.tensor(v, device=dev) for v in (alpha, lo, hi))
+    run.result(run.step(prec, da, dlo, dhi, r_obs=R_OBS_30), N_SWEEP)
+    flush.zero_()
+    torch.cuda.synchronize()
+    r = run.result(run.step(prec, da, dlo, dhi, r_obs=R_OBS_30), N_SWEEP)
+    ac = run.d_ac.cpu().numpy()
+    rel = np.abs(b_of(ac, R_OBS_30) - B_C) / B_C
+    sample = alpha[::64]
+    r64 = geon.shadow.trace(m, R_OBS_30, sample, STEP, MAX_STEPS, precision="fp64")
+    rmx = geon.shadow.trace(m, R_OBS_30, sample, STEP, MAX_STEPS, precision="mixed")
+    y0 = geon.shadow.equatorial_ray(m, R_OBS_30, sample)
+    rep = geon.accuracy.class_report(m, y0, STEP, MAX_STEPS, rmx.termination, r64.termination)
+    return {"workload": "schwarzschild shadow sweep at r_obs 30M: 2^20 rays alpha~U[5,15] deg + 64x40 bisections "
+                        "from lo~U[9,9.5], hi~U[9.8,10.3] deg, h 0.01, cap 200000, escape 1000M",
+            "ray_steps_per_s": r["steps"] / (r["ms"] / 1e3), "ms": r["ms"], "sweep_ms": r["sweep_ms"],
+            "bisection_ms": r["bisection_ms"], "b_c_rel_err_max": float(rel.max()),
+            "b_c_brackets_within_1e-6": int(np.sum(rel <= 1e-6)), "classes_vs_fp64": rep,
+            "sample_rays": int(len(sample))}
 
 
 def ctypes_peak(lib, fp64):
@@ -361,99 +809,6 @@ def load_traffic():
         return d.get("trace_mixed_shadow_bytes_per_launch")
     except (OSError, ValueError):
         return None
-
-
-def extra_legs(args, lib, geon, m, alpha, lo, hi, sweep_term, ac_run, prec, dev, value):
-    import torch
-    out = {}
-    # Accuracy of the mixed path against the FP64 path on a uniform sample (full traces).
-    k = args.fp64_sample
-    sample = alpha[::k]
-    y0 = geon.shadow.equatorial_ray(m, R_OBS, sample)
-    r64 = geon.trace(m, y0, STEP, MAX_STEPS, precision="fp64")
-    rmx = geon.trace(m, y0, STEP, MAX_STEPS, precision="mixed")
-    p64 = geon.shadow.physical_class(m, r64, MAX_STEPS)
-    pmx = geon.shadow.physical_class(m, rmx, MAX_STEPS)
-    esc = (p64 == 2) & (pmx == 2)
-    d64 = m.asymptotic_direction(r64.final_state[esc])
-    dmx = m.asymptotic_direction(rmx.final_state[esc])
-    ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0))
-    ac64, _, _, _ = geon.shadow.bisect(m, R_OBS, lo, hi, ITERS, STEP, MAX_STEPS, precision="fp64")
-    acm, _, _, _ = geon.shadow.bisect(m, R_OBS, lo, hi, ITERS, STEP, MAX_STEPS, precision="mixed")
-    vs_m, _, _, _ = geon.shadow.bisect(m, R_OBS, 0.0, np.pi / 2 - 1e-3, 60, STEP, MAX_STEPS, precision="mixed")
-    rel64 = np.abs(b_of(ac64) - B_C) / B_C
-    relm = np.abs(b_of(acm) - B_C) / B_C
-    out["accuracy"] = {
-        "sample_rays": int(len(sample)),
-        "class_mismatch_vs_fp64_raw": float(np.mean(rmx.termination != r64.termination)),
-        "class_mismatch_vs_fp64_physical": float(np.mean(pmx != p64)),
-        "fp64_rays_thrown_by_horizon_step": float(np.mean(p64 != r64.termination)),
-        "escape_dir_angle_err_rad_max": float(ang.max()) if ang.size else None,
-        "escape_dir_angle_err_rad_p50": float(np.median(ang)) if ang.size else None,
-        "null_drift_max_escaped_mixed": float(np.max(rmx.null_residual[esc])) if esc.any() else None,
-        "null_drift_max_escaped_fp64": float(np.max(r64.null_residual[esc])) if esc.any() else None,
-        "b_c_validate_shadow_bracket_mixed_rel_err": float(abs(b_of(vs_m[0]) - B_C) / B_C),
-        "b_c_brackets_within_1e-6_mixed": int(np.sum(relm <= 1e-6)),
-        "b_c_brackets_within_1e-6_fp64": int(np.sum(rel64 <= 1e-6)),
-        "b_c_rel_err_mixed_p50": float(np.median(relm)),
-        "b_c_rel_err_fp64_p50": float(np.median(rel64)),
-        "b_c_rel_err_fp64_max": float(rel64.max()),
-        "b_c_rel_err_mixed_max": float(relm.max()),
-        "b_c_this_run_rel_err_max": float(np.max(np.abs(b_of(ac_run) - B_C) / B_C)),
-    }
-    # e2e: the public host API, pinned host buffers, copies inside the timed region
-    pa = torch.tensor(alpha).pin_memory().numpy()
-    plo = torch.tensor(lo).pin_memory().numpy()
-    phi = torch.tensor(hi).pin_memory().numpy()
-    prec_name = "mixed" if prec == 1 else "fp64"
-    res = {}
-
-    def sweep():
-        res["sweep"] = geon.shadow.classify(m, R_OBS, pa, STEP, MAX_STEPS, precision=prec_name)
-
-    def bis():
-        res["bis"] = geon.shadow.bisect(m, R_OBS, plo, phi, ITERS, STEP, MAX_STEPS, precision=prec_name)
-
-    e2e_times, e2e_steps = [], 0
-    for i in range(2):
-        t0 = time.perf_counter()
-        th = threading.Thread(target=bis)
-        th.start()
-        sweep()
-        th.join()
-        dt = time.perf_counter() - t0
-        if i == 1:
-            e2e_times.append(dt)
-            e2e_steps = int(res["sweep"][1].sum()) + int(res["bis"][3].sum())
-    out["e2e"] = {"value": e2e_steps / float(np.mean(e2e_times)), "unit": "ray-steps/s",
-                  "h2d_bytes_per_step": N_SWEEP * 8 + 2 * N_BRACKETS * 8,
-                  "d2h_bytes_per_step": N_SWEEP * (4 + 8) + N_BRACKETS * (8 * 3 + 8),
-                  "api": "geon_shadow_classify + geon_shadow_bisect (host pointers, two threads)"}
-    # CPU baseline: the oracle (CPU restatement of the reference) on the host cores
-    from oracle import oracle as orc
-    threads = orc.hardware_threads()
-    rate, dt, st, ns = cpu_sample_rate(orc, alpha, args.cpu_rays, threads)
-    out["cpu_baseline"] = {"value": rate, "unit": "ray-steps/s", "cores": threads, "kind": "port",
-                           "sample": f"{ns} rays uniform over the sweep ({st} ray-steps, {dt:.1f} s)"}
-    return out
-
-
-def _wall(fn, reps):
-    """Best-of-reps wall time of fn() (host API calls return with results on the host)."""
-    best, out = 1e30, None
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        out = fn()
-        best = min(best, time.perf_counter() - t0)
-    return best, out
-
-
-def _emit(workload, value, unit, ms, dtype, extra):
-    line = {"metric": unit, "value": value, "unit": unit, "n_gpus": 1, "steps": 1, "warmup": 1,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": dtype, "data": "synthetic (seeded)", "config": {"workload": workload}}
-    line.update(extra)
-    print(json.dumps(line), flush=True)
 
 
 def reference_gpu_bar(width, height, r_obs, fov_deg, step, max_steps, reps=5):
@@ -506,201 +861,41 @@ def reference_gpu_bar(width, height, r_obs, fov_deg, step, max_steps, reps=5):
             "launch": f"{gx}x{gy} blocks of 16x16, best of {reps} after one warm-up, wall time around launch+sync"}
 
 
+def _emit(workload, value, unit, ms, dtype, extra):
+    line = {"metric": unit, "value": value, "unit": unit, "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": dtype, "data": "synthetic (seeded)", "config": {"workload": workload}}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
 def render_main(args):
-    """Schwarzschild 256^2 render (r 30M, fov 60, h 0.05, cap 20000, escape 100M, stars on):
-    FP64 and mixed through the host API, the oracle on every host core, and the
-    FP64 path at the reference CUDA program's own settings (escape 1000M)."""
+    """BASELINE config 1 as its own line (config1_leg)."""
     import geon_gb300 as geon
-    from oracle import oracle as orc
-    geon._load()
-    obs = [0.0, 30.0, np.pi / 2, 0.0]
-    cam = geon.Camera(obs, 60.0, 256, 256)
-    m = geon.Schwarzschild(1.0, 1.001, 100.0)
-    geon.autotune.autotune(m)
-    res = {}
-    for prec in ("fp64", "mixed"):
-        cfg = geon.RenderConfig(precision=prec, show_stars=True)
-        geon.render(m, cam, cfg)
-        dt, (rgb, st, cls, pst) = _wall(lambda: geon.render(m, cam, cfg, with_classes=True), 5)
-        res[prec] = {"ray_steps_per_s": st.total_steps / dt, "ms": 1e3 * dt, "total_steps": st.total_steps,
-                     "captured": st.captured, "escaped": st.escaped, "diverged": st.diverged, "cls": cls}
-    m1000 = geon.Schwarzschild(1.0, 1.001, 1000.0)
-    cfg = geon.RenderConfig(precision="fp64", show_stars=True)
-    geon.render(m1000, cam, cfg)
-    dt1000, (_, st1000) = _wall(lambda: geon.render(m1000, cam, cfg), 5)
-    ref_bar = reference_gpu_bar(256, 256, 30.0, 60.0, 0.05, 20000)
-    threads = orc.hardware_threads()
-    t0 = time.perf_counter()
-    _, ocls, opst, ost = orc.render(1, [1.0, 1.001, 100.0], obs, 60.0, 256, 256, 0.05, 20000, math=orc.LIBM,
-                                    nthreads=threads)
-    dt_cpu = time.perf_counter() - t0
-    cpu_rate = ost["total_steps"] / dt_cpu if "total_steps" in ost else float(opst.sum()) / dt_cpu
-    mism = float(np.mean(res["mixed"]["cls"] != res["fp64"]["cls"]))
-    exact = bool(np.array_equal(res["fp64"]["cls"], ocls))
-    for r in res.values():
-        r.pop("cls")
-    _emit("schwarzschild render 256x256, r_obs 30M, fov 60, h 0.05, cap 20000, escape 100M, stars on",
-          res["mixed"]["ray_steps_per_s"], "ray-steps/s", res["mixed"]["ms"], "f32 (mixed)",
-          {"render": res, "pixel_class_mismatch_mixed_vs_fp64": mism,
-           "fp64_pixel_classes_equal_oracle_libm": exact,
-           "reference_cuda_kernel_escape_1000M": ref_bar,
-           "fp64_escape_1000M": {"ms": 1e3 * dt1000, "total_steps": st1000.total_steps,
-                                 "ray_steps_per_s": st1000.total_steps / dt1000,
-                                 "captured": st1000.captured, "escaped": st1000.escaped,
-                                 "diverged": st1000.diverged,
-                                 "note": "the reference CUDA program's settings: 256x256 r 30 fov 60 h 0.05 "
-                                         "cap 20000, escape fixed at 1000M"},
-           "cpu_baseline": {"value": cpu_rate, "unit": "ray-steps/s", "cores": threads, "kind": "port",
-                            "sample": f"the full 256x256 image ({dt_cpu:.1f} s)"},
-           "timing": "host API wall time, best of 5, inputs and outputs on the host"})
+    lib = geon._load()
+    out = config1_leg(geon, lib, ctypes_peak(lib, 1))
+    mx = out["render"]["mixed"]
+    _emit(out["workload"], mx["ray_steps_per_s"], "ray-steps/s", mx["ms"], "f32 (mixed)",
+          {"config1": out, "timing": "host API wall time, best of 3, inputs and outputs on the host"})
 
 
 def exotic_main(args):
-    """2048^2 Alcubierre (R 2, thickness 0.125, v 0.5, observer x = -10 looking +x)
-    and Morris-Thorne (b0 1, observer l = 10) renders, fov 90, h 0.05, cap 20000:
-    mixed on the full image; FP64 on every 16th row; the oracle on one row."""
+    """BASELINE config 3 as its own line (config3_leg)."""
     import geon_gb300 as geon
-    from oracle import oracle as orc
-    geon._load()
-    cases = {"alcubierre": (geon.Alcubierre(2.0, 0.125, 0.5, 0.0), 2, [2.0, 0.125, 0.5, 0.0],
-                            [0.0, -10.0, 0.0, 0.0], -1),
-             "morris_thorne": (geon.MorrisThorne(1.0), 3, [1.0], [0.0, 10.0, np.pi / 2, 0.0], 1)}
-    n = args.size
-    out = {}
-    threads = orc.hardware_threads()
-    for name, (m, kind, params, obs, fwd) in cases.items():
-        geon.autotune.autotune(m)
-        cam = geon.Camera(obs, 90.0, n, n, forward_sign=fwd)
-        cfg = geon.RenderConfig(precision="mixed", show_stars=True)
-        geon.render(m, geon.Camera(obs, 90.0, 64, 64, forward_sign=fwd), cfg)
-        dt, (_, st) = _wall(lambda: geon.render(m, cam, cfg), 1)
-        tet = cam.tetrad(m)
-        rows = np.arange(0, n, 16)
-        y0 = cam.ray_states(tet).reshape(n, n, 8)[rows].reshape(-1, 8)
-        t0 = time.perf_counter()
-        r64 = geon.trace(m, y0, 0.05, 20000, precision="fp64")
-        dt64 = time.perf_counter() - t0
-        rmx = geon.trace(m, y0, 0.05, 20000, precision="mixed")
-        p64, pmx = r64.termination, rmx.termination
-        esc = (p64 == 2) & (pmx == 2)
-        d64 = m.asymptotic_direction(r64.final_state[esc])
-        dmx = m.asymptotic_direction(rmx.final_state[esc])
-        ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0)) if esc.any() else np.zeros(1)
-        yc = y0[: n]  # the first sampled row
-        t0 = time.perf_counter()
-        _, _, osteps, _ = orc.trace(kind, params, yc, 0.05, 20000, math=orc.LIBM, nthreads=threads)
-        dt_cpu = time.perf_counter() - t0
-        out[name] = {"mixed_ray_steps_per_s": st.total_steps / dt, "mixed_ms": 1e3 * dt,
-                     "mixed_total_steps": st.total_steps,
-                     "fp64_ray_steps_per_s": float(r64.steps_taken.sum()) / dt64,
-                     "fp64_sample": f"every 16th row ({len(y0)} rays), host API wall time",
-                     "mixed_over_fp64": (st.total_steps / dt) / (float(r64.steps_taken.sum()) / dt64),
-                     "class_mismatch_mixed_vs_fp64": float(np.mean(p64 != pmx)),
-                     "escape_dir_err_rad_p50": float(np.median(ang)), "escape_dir_err_rad_max": float(ang.max()),
-                     "cpu_baseline": {"value": float(osteps.sum()) / dt_cpu, "unit": "ray-steps/s", "cores": threads,
-                                      "kind": "port", "sample": f"row 0 ({len(yc)} rays, {dt_cpu:.1f} s)"}}
-    v = sum(o["mixed_total_steps"] for o in out.values()) / sum(o["mixed_ms"] / 1e3 for o in out.values())
-    _emit(f"exotic renders {n}x{n}: alcubierre (R 2, thickness 0.125, v 0.5) and morris-thorne (b0 1), fov 90, "
-          "h 0.05, cap 20000", v, "ray-steps/s", sum(o["mixed_ms"] for o in out.values()), "f32 (mixed)",
-          {"exotic": out, "timing": "host API wall time"})
-
-
-def curvature_cpu_leg(orc, params, pts, threads, budget_s=8.0):
-    """The config-4 job per grid point (Einstein tensor + T(k, k) for 16 null
-    vectors) on the oracle, on a uniform sample of the grid sized to about
-    budget_s each: once with the reference's call graph (Riemann formed again
-    inside every curvature.rs call: twice for the Einstein tensor, twice per
-    vector for T(k, k)) and once with Riemann formed once per point (the same
-    bits). The cost does not depend on the vectors' values, so 16 copies of the
-    reference's own k = (1, 1, 0, 0) stand in for them."""
-    k = np.tile([[1.0, 1.0, 0.0, 0.0]], (16, 1))
-    out = {}
-    for name, faithful in (("reference_call_graph", True), ("riemann_once", False)):
-        def run(m):
-            sub = pts[np.linspace(0, len(pts) - 1, m).astype(np.int64)]
-            t0 = time.perf_counter()
-            orc.curvature(2, params, sub, "einstein", math=orc.LIBM, faithful=faithful, nthreads=threads)
-            orc.nec(2, params, sub, k, math=orc.LIBM, faithful=faithful, nthreads=threads)
-            return time.perf_counter() - t0
-        m = min(len(pts), 256)
-        dt = run(m)
-        m = int(min(len(pts), max(m, m * budget_s / max(dt, 1e-6))))
-        dt = run(m)
-        out[name] = {"value": m / dt, "points": m, "seconds": dt}
-    return out
+    lib = geon._load()
+    out = config3_leg(geon, lib, args.size, args.row_step)
+    _emit(out["workload"], out["mixed_ray_steps_per_s_both"], "ray-steps/s",
+          sum(out[c]["mixed_ms"] for c in ("alcubierre", "morris_thorne")), "f32 (mixed)",
+          {"config3": out, "timing": "host API wall time"})
 
 
 def curvature_main(args):
-    """Curvature grid jobs (FP64): 128^3 Alcubierre (v_s 0.5, R 2, sigma 8)
-    Einstein + T(k,k) for 16 null vectors per point; a 4096-point Morris-Thorne
-    line; 1e5 Schwarzschild vacuum points (Ricci scalar)."""
+    """BASELINE config 4 as its own line (config4_leg)."""
     import geon_gb300 as geon
-    from oracle import oracle as orc
-    geon._load()
-    threads = orc.hardware_threads()
-    alc = geon.Alcubierre(2.0, 0.125, 0.5, 0.0)  # R 2, thickness 1/sigma, sigma 8, v_s 0.5
-    n = args.grid
-    geon.curvature.grid(alc, (-4, -4, -4), (4, 4, 4), (8, 8, 8), nk=16)
-    dt, (pts, ein, nec, _) = _wall(lambda: geon.curvature.grid(alc, (-4, -4, -4), (4, 4, 4), (n, n, n), nk=16), 2)
-    sub = np.arange(0, len(pts), max(1, len(pts) // 2048))
-    t0 = time.perf_counter()
-    oein = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.GEON, nthreads=threads)
-    dt_cpu = time.perf_counter() - t0
-    bit_exact = bool(np.array_equal(oein.reshape(-1, 16), ein[sub].reshape(-1, 16)))
-    oein_libm = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.LIBM, nthreads=threads)
-    err_libm = float(np.max(np.abs(oein_libm.reshape(-1, 16) - ein[sub].reshape(-1, 16))))
-    bit_exact_libm = bool(np.array_equal(oein_libm.reshape(-1, 16), ein[sub].reshape(-1, 16)))
-    cpu = curvature_cpu_leg(orc, [2.0, 0.125, 0.5, 0.0], pts, threads)
-    # Kernel-only leg: the same grid job through the device-pointer entry
-    # point, outputs resident in HBM (537 MB at 128^3, larger than L2), CUDA
-    # events on the launching stream.
-    import torch
-    st = torch.cuda.current_stream()
-    ein_d = torch.empty(len(pts) * 16, dtype=torch.float64, device="cuda")
-    nec_d = torch.empty(len(pts) * 16, dtype=torch.float64, device="cuda")
-    launch = lambda: geon.curvature.grid_dev(alc, (-4, -4, -4), (4, 4, 4), (n, n, n), ein_d, nec_d, nk=16,
-                                             stream=st.cuda_stream)
-    for _ in range(3):
-        launch()
-    reps = 5
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(st)
-    for _ in range(reps):
-        launch()
-    e1.record(st)
-    torch.cuda.synchronize()
-    kernel_ms = e0.elapsed_time(e1) / reps
-    dev_same = bool(np.array_equal(ein_d.cpu().numpy().reshape(-1, 16), ein.reshape(-1, 16))
-                    and np.array_equal(nec_d.cpu().numpy().reshape(-1, 16), nec.reshape(-1, 16)))
-    del ein_d, nec_d
-    mt = geon.MorrisThorne(1.0)
-    dt_mt, (mpts, mein, mnec, _) = _wall(lambda: geon.curvature.grid(mt, (-5, np.pi / 2, 0), (5, np.pi / 2, 0),
-                                                                     (4096, 1, 1), nk=16), 3)
-    rng = np.random.default_rng(7)
-    x = np.stack([np.zeros(100000), rng.uniform(3.0, 30.0, 100000), rng.uniform(0.3, 2.8, 100000),
-                  rng.uniform(0.0, 6.2, 100000)], axis=1)
-    sch = geon.Schwarzschild(1.0)
-    dt_s, rs = _wall(lambda: geon.curvature.ricci_scalar(sch, x), 3)
-    _emit(f"curvature grid {n}^3 alcubierre (v_s 0.5, R 2, sigma 8) einstein + 16 null T(k,k) per point",
-          len(pts) / dt, "grid-points/s", 1e3 * dt, "f64",
-          {"curvature": {"alcubierre_grid": {"points": len(pts), "ms": 1e3 * dt, "points_per_s": len(pts) / dt,
-                                             "kernel_ms": kernel_ms,
-                                             "kernel_points_per_s": len(pts) / (1e-3 * kernel_ms),
-                                             "device_api_same_bits": dev_same,
-                                             "bit_exact_vs_oracle_geon_sample": bit_exact,
-                                             "max_abs_diff_vs_oracle_libm": err_libm,
-                                             "bit_exact_vs_oracle_libm_sample": bit_exact_libm},
-                         "morris_thorne_line": {"points": 4096, "ms": 1e3 * dt_mt, "points_per_s": 4096 / dt_mt,
-                                                "T_tt_throat_check": "tests/test_gpu_curvature_grid.py"},
-                         "schwarzschild_vacuum": {"points": 100000, "ms": 1e3 * dt_s, "points_per_s": 1e5 / dt_s,
-                                                  "max_abs_ricci_scalar": float(np.max(np.abs(rs)))}},
-           "cpu_baseline": {"value": cpu["reference_call_graph"]["value"], "unit": "grid-points/s", "cores": threads,
-                            "kind": "port",
-                            "sample": (f"{cpu['reference_call_graph']['points']} grid points, Einstein + 16 T(k,k) each, "
-                                       f"curvature.rs call graph ({cpu['reference_call_graph']['seconds']:.1f} s)"),
-                            "riemann_once": cpu["riemann_once"]},
-           "timing": "host API wall time (includes the copy of results to the host)"})
+    lib = geon._load()
+    out = config4_leg(geon, args.grid, ctypes_peak(lib, 1), cpu_budget_s=8.0)
+    _emit(out["workload"], out["points_per_s"], "grid-points/s", out["host_api_ms"], "f64",
+          {"config4": out, "timing": "host API wall time (includes the copy of results to the host)"})
 
 
 SERVE_RES = (128, 256, 512, 1024, 2048)
@@ -831,6 +1026,7 @@ if __name__ == "__main__":
         ap.add_argument("--serve-precisions", default="mixed",
                         help="comma list; the fp64 stream of 200 requests runs for tens of minutes")
         ap.add_argument("--size", type=int, default=2048, help="exotic: image side")
+        ap.add_argument("--row-step", type=int, default=16, help="exotic: FP64 traces every k-th row")
         ap.add_argument("--grid", type=int, default=128, help="curvature: grid side")
         ap.add_argument("--gpus", type=int, default=1)
         ap.add_argument("--steps", type=int, default=1)

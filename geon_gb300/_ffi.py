@@ -54,6 +54,12 @@ class GeonRenderStats(ctypes.Structure):
                 ("avg_steps", ctypes.c_double), ("total_steps", ctypes.c_int64)]
 
 
+class GeonRenderItem(ctypes.Structure):
+    _fields_ = [("metric", ctypes.c_void_p), ("camera", GeonCamera), ("render", GeonRenderConfig),
+                ("rgb", ctypes.c_void_p), ("stats", ctypes.POINTER(GeonRenderStats)),
+                ("pixel_class", ctypes.c_void_p), ("pixel_steps", ctypes.c_void_p)]
+
+
 class GeonJob(ctypes.Structure):
     """geon_job: one serving request (pointers are plain addresses)."""
     _fields_ = [("type", ctypes.c_int32), ("metric_kind", ctypes.c_int32),
@@ -112,6 +118,7 @@ SIGNATURES = {
     "geon_tonemap_u8_dev": (ctypes.c_int, [c_void_p, c_size_t, c_void_p, c_void_p]),
     "geon_render_ex": (ctypes.c_int, [c_void_p, ctypes.POINTER(GeonCamera), ctypes.POINTER(GeonRenderConfig),
                                       c_float_p, ctypes.POINTER(GeonRenderStats), c_int32_p, c_int64_p]),
+    "geon_render_batch": (ctypes.c_int, [ctypes.POINTER(GeonRenderItem), c_size_t]),
     "geon_sky_sample": (ctypes.c_int, [c_double_p, c_size_t, ctypes.c_int, c_float_p]),
     "geon_set_show_stars": (None, [ctypes.c_int]),
     "geon_get_show_stars": (ctypes.c_int, []),
@@ -142,6 +149,9 @@ SIGNATURES = {
     "geon_equatorial_rays": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_size_t, c_double_p]),
     "geon_shadow_classify": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_size_t, ctypes.c_double,
                                             ctypes.c_int64, ctypes.c_int, c_int32_p, c_int64_p]),
+    "geon_shadow_trace": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_size_t, ctypes.c_double,
+                                         ctypes.c_int64, ctypes.c_int, c_int32_p, c_double_p, c_int64_p,
+                                         c_double_p]),
     "geon_shadow_bisect": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_double_p, c_size_t,
                                           ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
                                           c_double_p, c_double_p, c_double_p, c_int64_p]),

@@ -28,6 +28,7 @@ UNITS = [
     ("trace_fp64.cu", ["--fmad=false"]),
     ("trace_mixed.cu", ["--fmad=false"]),
     ("trace_adaptive.cu", ["--fmad=false"]),
+    ("trace_fp64fast.cu", ["--fmad=false"]),
     ("curvature_fp64.cu", ["--fmad=false"]),
     ("capi.cu", ["--fmad=false"]),
     ("noalloc.cu", ["--fmad=false"]),
@@ -101,7 +102,7 @@ def build_library(force=False, verbose=False):
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
         return obj, r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(UNITS))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(16, len(UNITS), os.cpu_count() or 8)) as ex:
         results = list(ex.map(compile_unit, UNITS))
     if verbose:
         for _, log in results:

@@ -29,7 +29,7 @@ std::atomic<int> g_show_stars{1};
 // M, b0, s; 0 disables) and the null re-projection switch.
 std::atomic<float> g_band[4] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
 std::atomic<int> g_reproject{0};
-std::atomic<int> g_orbit{0};
+std::atomic<int> g_orbit{1};  // orbit-plane frame of the mixed path (default on)
 std::atomic<float> g_reserve{0.0f};
 std::atomic<double> g_rtol{1e-10};  // GEON_ADAPTIVE error tolerances
 std::atomic<double> g_atol{1e-12};
@@ -155,10 +155,13 @@ cudaError_t launch_trace(const TraceLaunch& L0, int precision, int src, int sink
   if (src == SRC_EQUATORIAL) L.variant = g_variant[L.M.kind][1].load();
   if (precision == GEON_MIXED) return launch_trace_mixed(L, src, sink, s);
   if (precision == GEON_ADAPTIVE) return launch_trace_adaptive(L, src, sink, s);
+  if (precision == GEON_FP64_FAST) return launch_trace_fp64fast(L, src, sink, s);
   return launch_trace_fp64(L, src, sink, s);
 }
 
-bool valid_precision(int p) { return p == GEON_FP64 || p == GEON_MIXED || p == GEON_ADAPTIVE; }
+bool valid_precision(int p) {
+  return p == GEON_FP64 || p == GEON_MIXED || p == GEON_ADAPTIVE || p == GEON_FP64_FAST;
+}
 
 // The precision is known and has a stepper for this metric.
 int check_precision(geon_metric_t m, int p) {
@@ -714,6 +717,105 @@ int geon_render_u8(geon_metric_t m, const geon_camera* cam, const geon_render_co
   return render_any(m, cam, cfg, rgb, rgb8, stats, nullptr, nullptr);
 }
 
+int geon_render_batch(const geon_render_item* items, size_t n) {
+  if (n == 0) return GEON_OK;
+  if (!items || n > (size_t)MULTI_MAX_JOBS) return fail(GEON_ERR_INVALID, "geon_render_batch takes 1 to 8 items");
+  const int precision = items[0].render.precision;
+  if (precision != GEON_FP64 && precision != GEON_MIXED)
+    return fail(GEON_ERR_INVALID, "geon_render_batch runs GEON_FP64 or GEON_MIXED");
+  for (size_t j = 0; j < n; ++j) {
+    const geon_render_item& it = items[j];
+    if (int rc = check_metric(it.metric)) return rc;
+    if (it.render.precision != precision) return fail(GEON_ERR_INVALID, "every item of a batch needs one precision");
+    if (it.metric->desc.kind == GEON_FIELD) return fail(GEON_ERR_UNSUPPORTED, "geon_render_batch: no sampled metrics");
+    if (!it.rgb) return fail(GEON_ERR_INVALID, "null buffer");
+    if (it.render.max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
+  }
+  cudaStream_t s = host_stream();
+  struct Bufs {
+    DBuf srgb, term, steps, res, rgb, cls, pst;
+    int64_t npix = 0, spa = 1;
+  };
+  std::vector<Bufs> B(n);
+  std::vector<TraceLaunch> jobs(n);
+  MultiDesc D;
+  std::memset(&D, 0, sizeof D);
+  D.njobs = (int)n;
+  DBuf ws, djobs;
+  const size_t ws_bytes = sizeof(unsigned long long) * (2 + 6 * n);
+  GEON_CUDA(ws.alloc(ws_bytes, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, ws_bytes, s));
+  unsigned long long* wsu = ws.as<unsigned long long>();
+  for (size_t j = 0; j < n; ++j) {
+    const geon_render_item& it = items[j];
+    Bufs& b = B[j];
+    b.spa = it.render.samples_per_axis < 1 ? 1 : it.render.samples_per_axis;
+    CameraDesc c;
+    if (int rc = make_camera(it.metric, &it.camera, b.spa, c, s)) return rc;
+    b.npix = it.camera.width * it.camera.height;
+    const int64_t nsamp = b.npix * b.spa * b.spa;
+    GEON_CUDA(b.srgb.alloc(sizeof(float) * 3 * nsamp, s));
+    GEON_CUDA(b.term.alloc(sizeof(int32_t) * nsamp, s));
+    GEON_CUDA(b.steps.alloc(sizeof(int64_t) * nsamp, s));
+    GEON_CUDA(b.res.alloc(sizeof(double) * nsamp, s));
+    GEON_CUDA(b.rgb.alloc(sizeof(float) * 3 * b.npix, s));
+    GEON_CUDA(b.cls.alloc(sizeof(int32_t) * b.npix, s));
+    GEON_CUDA(b.pst.alloc(sizeof(int64_t) * b.npix, s));
+    TraceLaunch L = base_launch(it.metric, it.render.step, it.render.max_steps);
+    L.cam = c;
+    L.n = nsamp;
+    L.term = b.term.as<int32_t>();
+    L.steps = b.steps.as<int64_t>();
+    L.resid = b.res.as<double>();
+    L.srgb = b.srgb.as<float>();
+    L.show_stars = it.render.show_stars < 0 ? g_show_stars.load() : (it.render.show_stars != 0);
+    for (int q = 0; q < 3; ++q) {
+      L.captured_rgb[q] = it.render.captured_rgb[q];
+      L.diverged_rgb[q] = it.render.diverged_rgb[q];
+    }
+    L.queue = wsu;
+    L.flags = reinterpret_cast<int*>(wsu + 1);
+    jobs[j] = L;
+    D.start[j + 1] = D.start[j] + nsamp;
+  }
+  D.queue = wsu;
+  GEON_CUDA(djobs.alloc(sizeof(TraceLaunch) * n, s));
+  GEON_CUDA(cudaMemcpyAsync(djobs.p, jobs.data(), sizeof(TraceLaunch) * n, cudaMemcpyHostToDevice, s));
+  counted();
+  if (precision == GEON_MIXED) GEON_CUDA(launch_trace_multi_mixed(djobs.as<TraceLaunch>(), D, g_reserve.load(), s));
+  else GEON_CUDA(launch_trace_multi_fp64(djobs.as<TraceLaunch>(), D, g_reserve.load(), s));
+  std::vector<unsigned long long> hst(6 * n);
+  for (size_t j = 0; j < n; ++j) {
+    const geon_render_item& it = items[j];
+    Bufs& b = B[j];
+    unsigned long long* dstats = wsu + 2 + 6 * j;
+    counted();
+    GEON_CUDA(launch_render_reduce(b.srgb.as<float>(), b.term.as<int32_t>(), b.steps.as<int64_t>(),
+                                   b.res.as<double>(), b.npix, b.spa, b.rgb.as<float>(), b.cls.as<int32_t>(),
+                                   b.pst.as<int64_t>(), dstats, s));
+    GEON_CUDA(cudaMemcpyAsync(it.rgb, b.rgb.p, sizeof(float) * 3 * b.npix, cudaMemcpyDeviceToHost, s));
+    if (int rc = copy_out(it.pixel_class, b.cls.p, sizeof(int32_t) * b.npix, s)) return rc;
+    if (int rc = copy_out(it.pixel_steps, b.pst.p, sizeof(int64_t) * b.npix, s)) return rc;
+    GEON_CUDA(cudaMemcpyAsync(&hst[6 * j], dstats, sizeof(unsigned long long) * 6, cudaMemcpyDeviceToHost, s));
+  }
+  int flags = 0;
+  if (int rc = sync_and_flags(s, reinterpret_cast<int*>(wsu + 1), &flags)) return rc;
+  for (size_t j = 0; j < n; ++j) {
+    geon_render_stats* st = items[j].stats;
+    if (!st) continue;
+    const unsigned long long* h = &hst[6 * j];
+    st->captured = (int64_t)h[0];
+    st->escaped = (int64_t)h[1];
+    st->diverged = (int64_t)h[2];
+    double mr;
+    std::memcpy(&mr, &h[4], sizeof mr);
+    st->max_null_residual = mr;
+    st->avg_steps = (double)(int64_t)h[3] / (double)B[j].npix;
+    st->total_steps = (int64_t)h[5];
+  }
+  return singular_status(flags);
+}
+
 int geon_tonemap_u8_dev(const float* rgb, size_t n, uint8_t* out, void* stream) {
   if (n == 0) return GEON_OK;
   if (!rgb || !out) return fail(GEON_ERR_INVALID, "null buffer");
@@ -848,6 +950,43 @@ int geon_shadow_classify(geon_metric_t m, double r_obs, const double* alpha, siz
     return rc;
   GEON_CUDA(cudaMemcpyAsync(term, dt.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
   if (int rc = copy_out(steps, dst.p, sizeof(int64_t) * n, s)) return rc;
+  GEON_CUDA(cudaStreamSynchronize(s));
+  return GEON_OK;
+}
+
+int geon_shadow_trace(geon_metric_t m, double r_obs, const double* alpha, size_t n, double step,
+                      int64_t max_steps, int precision, int32_t* term, double* final_state, int64_t* steps,
+                      double* null_residual) {
+  if (int rc = check_metric(m)) return rc;
+  if (m->desc.kind != GEON_SCHWARZSCHILD) return fail(GEON_ERR_INVALID, "equatorial rays need a Schwarzschild metric");
+  if (!valid_precision(precision)) return fail(GEON_ERR_INVALID, "unknown precision");
+  if (n == 0) return GEON_OK;
+  if (!alpha || !term) return fail(GEON_ERR_INVALID, "null buffer");
+  cudaStream_t s = host_stream();
+  DBuf da, dt, dy, dst, dr, ws;
+  GEON_CUDA(da.alloc(sizeof(double) * n, s));
+  GEON_CUDA(dt.alloc(sizeof(int32_t) * n, s));
+  GEON_CUDA(dy.alloc(sizeof(double) * 8 * n, s));
+  GEON_CUDA(dst.alloc(sizeof(int64_t) * n, s));
+  GEON_CUDA(dr.alloc(sizeof(double) * n, s));
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 2, s));
+  GEON_CUDA(cudaMemcpyAsync(da.p, alpha, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 2, s));
+  TraceLaunch L = base_launch(m, step, max_steps);
+  L.n = (int64_t)n;
+  L.alpha = da.as<double>();
+  L.r_obs = r_obs;
+  L.term = dt.as<int32_t>();
+  L.yfinal = dy.as<double>();
+  L.steps = dst.as<int64_t>();
+  L.resid = dr.as<double>();
+  L.queue = ws.as<unsigned long long>();
+  L.flags = reinterpret_cast<int*>(L.queue + 1);
+  GEON_CUDA(launch_trace(L, precision, SRC_EQUATORIAL, SINK_TRACE, s));
+  GEON_CUDA(cudaMemcpyAsync(term, dt.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  if (int rc = copy_out(final_state, dy.p, sizeof(double) * 8 * n, s)) return rc;
+  if (int rc = copy_out(steps, dst.p, sizeof(int64_t) * n, s)) return rc;
+  if (int rc = copy_out(null_residual, dr.p, sizeof(double) * n, s)) return rc;
   GEON_CUDA(cudaStreamSynchronize(s));
   return GEON_OK;
 }

@@ -31,6 +31,14 @@
 // constants are the published ones (ln 2 split so that k * EX_LN2_HI is exact).
 // This file must be compiled without mul+add contraction (--fmad=false); the
 // fma() calls below are the only fused operations.
+//
+// The expm1/tanh method, its range thresholds and its constants follow fdlibm,
+// whose notice is kept here as its licence asks:
+//   Copyright (C) 1993 by Sun Microsystems, Inc. All rights reserved.
+//   Developed at SunSoft, a Sun Microsystems, Inc. business.
+//   Permission to use, copy, modify, and distribute this
+//   software is freely granted, provided that this notice
+//   is preserved.
 #pragma once
 
 namespace geon {

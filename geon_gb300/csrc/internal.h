@@ -115,6 +115,19 @@ inline int64_t persistent_slots(int sms, int per_sm, float reserve) {
 }
 
 cudaError_t launch_trace_adaptive(const TraceLaunch& L, int src, int sink, cudaStream_t s);
+// ---- one persistent launch over several renders (trace_fp64.cu, trace_mixed.cu) ----
+// Job j of the launch owns the global ray indices [start[j], start[j+1]) of its
+// one work queue (trace_loop_multi in trace_common.cuh).
+constexpr int MULTI_MAX_JOBS = 8;
+struct MultiDesc {
+  int njobs;
+  int64_t start[MULTI_MAX_JOBS + 1];
+  unsigned long long* queue;
+};
+cudaError_t launch_trace_multi_fp64(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s);
+cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s);
+// ---- launchers (trace_fp64fast.cu) ----
+cudaError_t launch_trace_fp64fast(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 // rgb and rgb8 (the tonemapped bytes) may each be null
 cudaError_t launch_render_reduce(const float* srgb, const int32_t* term, const int64_t* steps,
                                  const double* resid, int64_t npix, int64_t spa, float* rgb,

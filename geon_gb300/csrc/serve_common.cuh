@@ -95,6 +95,7 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
             n = e.n;
             st.restore(jobs[slot].L, e.w, n);
             st.set_source(jobs[slot].src);
+            st.resume_frame(jobs[slot].L, ray);
           }
         }
       }
@@ -140,8 +141,8 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
           else if (J.src == SRC_EQUATORIAL) serve_load<K, SRC_EQUATORIAL>(J.L, ray, y0);
           else serve_load<K, SRC_ARRAY>(J.L, ray, y0);
           st.rebind(J.L);
-          st.load(J.L, y0);
           st.set_source(J.src);
+          st.load(J.L, y0);
         }
       }
       need = __ballot_sync(FULL, slot < 0);

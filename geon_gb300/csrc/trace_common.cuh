@@ -184,4 +184,99 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
   st.finish(L);
 }
 
+
+// ---------------------------------------------------------------------------
+// Several jobs in one persistent launch (e.g. renders of different metrics):
+// one work queue over the concatenated rays, job j owning the global indices
+// [start[j], start[j+1]). A lane that takes a ray finds its job by the offsets
+// (a few compares: at most MULTI_MAX_JOBS jobs) and steps it with that job's
+// metric, camera and outputs; the job table is in global memory (L1-resident).
+// ---------------------------------------------------------------------------
+// store_ray for a ray of metric kind `kind` (known at run time).
+template <int SINK>
+__device__ __forceinline__ void store_ray_any(const TraceLaunch& L, int kind, int64_t ray, int term,
+                                              const double y[8], int64_t steps) {
+  switch (kind) {
+    case KIND_SCHWARZSCHILD: store_ray<KIND_SCHWARZSCHILD, SINK>(L, ray, term, y, steps); return;
+    case KIND_ALCUBIERRE: store_ray<KIND_ALCUBIERRE, SINK>(L, ray, term, y, steps); return;
+    case KIND_MORRIS_THORNE: store_ray<KIND_MORRIS_THORNE, SINK>(L, ray, term, y, steps); return;
+    default: store_ray<KIND_MINKOWSKI, SINK>(L, ray, term, y, steps); return;
+  }
+}
+
+// trace_loop over the rays of several jobs. Stepper additionally provides
+// bind(L, src): take the constants and metric kind of job L for the next ray.
+template <class Stepper, int SRC, int SINK>
+__device__ __forceinline__ void trace_loop_multi(const TraceLaunch* __restrict__ jobs, const MultiDesc& D) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const unsigned long long total = (unsigned long long)D.start[D.njobs];
+  int job = -1;
+  int64_t ray = 0;
+  int64_t n = 0;
+  Stepper st;
+  bool queue_open = true;
+  for (;;) {
+    const unsigned need = __ballot_sync(FULL, job < 0);
+    if (need && queue_open) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(D.queue, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (base + __popc(need) >= total) queue_open = false;
+      if (job < 0) {
+        const unsigned long long idx = base + __popc(need & lt_mask);
+        if (idx < total) {
+          int j = 0;
+          while (j + 1 < D.njobs && (int64_t)idx >= D.start[j + 1]) ++j;
+          job = j;
+          ray = (int64_t)idx - D.start[j];
+          n = 0;
+          const TraceLaunch& L = jobs[j];
+          double y0[8];
+          load_ray<SRC>(L, ray, y0);
+          st.bind(L, SRC);
+          st.load(L, y0);
+        }
+      }
+    }
+    if (__ballot_sync(FULL, job >= 0) == 0) break;
+    if (job >= 0) {
+      const TraceLaunch& L = jobs[job];
+      const int64_t max_steps = L.max_steps;
+#pragma unroll 1
+      for (int inner = 0; inner < TRACE_INNER; ++inner) {
+        int t = TERM_NONE;
+        int64_t taken = n;
+        if (n >= max_steps) {
+          t = TERM_DIVERGED;
+          taken = max_steps;
+        } else {
+          t = st.terminate(L);
+          if (t == TERM_NONE) {
+            const int r = st.step(L);
+            if (r == STEP_OK) {
+              ++n;
+            } else if (r == STEP_NONFINITE) {
+              t = TERM_DIVERGED;
+            } else {
+              t = TERM_CAPTURED;
+              taken = n + 1;
+            }
+          }
+        }
+        if (t != TERM_NONE) {
+          double y[8];
+          st.to_double(y);
+          store_ray_any<SINK>(L, L.M.kind, ray, t, y, taken);
+          job = -1;
+          break;
+        }
+      }
+    }
+  }
+  st.finish(jobs[0]);
+}
+
 }  // namespace geon

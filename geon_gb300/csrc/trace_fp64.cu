@@ -58,7 +58,77 @@ struct Fp64Stepper {
   }
   __device__ __forceinline__ void rebind(const TraceLaunch&) {}
   __device__ __forceinline__ void set_source(int) {}
+  __device__ __forceinline__ void resume_frame(const TraceLaunch&, int64_t) {}
 };
+
+// The FP64 stepper of a launch whose rays have different metric kinds (one
+// persistent kernel over several renders): the kind is the lane's current
+// ray's, and every call branches on it.
+struct Fp64StepperAny {
+  double y[8];
+  int kind = KIND_MINKOWSKI;
+  bool singular = false;
+  __device__ __forceinline__ void bind(const TraceLaunch& L, int) { kind = L.M.kind; }
+  __device__ __forceinline__ void load(const TraceLaunch&, const double y0[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = y0[i];
+  }
+  __device__ __forceinline__ void to_double(double out[8]) const {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = y[i];
+  }
+  __device__ __forceinline__ int terminate(const TraceLaunch& L) const {
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: return metric_terminate<KIND_SCHWARZSCHILD>(L.M, y);
+      case KIND_ALCUBIERRE: return metric_terminate<KIND_ALCUBIERRE>(L.M, y);
+      case KIND_MORRIS_THORNE: return metric_terminate<KIND_MORRIS_THORNE>(L.M, y);
+      default: return metric_terminate<KIND_MINKOWSKI>(L.M, y);
+    }
+  }
+  __device__ __forceinline__ int step(const TraceLaunch& L) {
+    double yn[8];
+    bool ok;
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: ok = rk4_step<KIND_SCHWARZSCHILD>(L.M, y, L.step, L.half_step, L.sixth, yn); break;
+      case KIND_ALCUBIERRE: ok = rk4_step<KIND_ALCUBIERRE>(L.M, y, L.step, L.half_step, L.sixth, yn); break;
+      case KIND_MORRIS_THORNE: ok = rk4_step<KIND_MORRIS_THORNE>(L.M, y, L.step, L.half_step, L.sixth, yn); break;
+      default: ok = rk4_step<KIND_MINKOWSKI>(L.M, y, L.step, L.half_step, L.sixth, yn); break;
+    }
+    singular |= !ok;
+    bool finite = true;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) finite &= isfinite(yn[i]);
+    if (!finite) return STEP_NONFINITE;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = yn[i];
+    return STEP_OK;
+  }
+  __device__ __forceinline__ void finish(const TraceLaunch& L) {
+    if (singular) atomicOr(L.flags, 1);
+  }
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK) trace_multi_fp64_kernel(const TraceLaunch* jobs, const MultiDesc D) {
+  trace_loop_multi<Fp64StepperAny, SRC_CAMERA, SINK_RENDER>(jobs, D);
+}
+
+cudaError_t launch_trace_multi_fp64(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s) {
+  static int sms = 0, per_sm = 0;
+  if (sms == 0) {
+    int dev = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_multi_fp64_kernel, TRACE_BLOCK, 0);
+    per_sm = occ < 1 ? 1 : occ;
+  }
+  const int64_t n = D.start[D.njobs];
+  if (n <= 0) return cudaSuccess;
+  const int64_t slots = persistent_slots(sms, per_sm, reserve);
+  const int64_t need = (n + TRACE_BLOCK - 1) / TRACE_BLOCK;
+  const int grid = (int)(need < slots ? need : slots);
+  trace_multi_fp64_kernel<<<grid < 1 ? 1 : grid, TRACE_BLOCK, 0, s>>>(jobs, D);
+  return cudaGetLastError();
+}
 
 template <int K, int SRC, int SINK>
 __global__ void __launch_bounds__(TRACE_BLOCK) trace_fp64_kernel(const TraceLaunch L) {

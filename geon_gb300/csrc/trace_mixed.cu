@@ -61,10 +61,12 @@ __device__ __forceinline__ bool ff_gt(float hi, float lo, float thi, float tlo) 
 // FEAT_PLANAR: every ray is an equatorial Schwarzschild ray (theta = pi/2,
 // p^theta = 0, bin/validate_shadow.rs:20-35); FEAT_PLANAR_DYN: a per-ray flag
 // says so (the serving kernel, whose lanes take rays of any job). FEAT_ORBIT
-// (opt-in, MIXED_ORBIT): rays of a spherically symmetric metric (Schwarzschild,
-// Morris-Thorne) are turned into the frame of their own orbit plane at load,
-// stepped there on the equator, and turned back at the end.
-enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2, FEAT_PLANAR = 4, FEAT_PLANAR_DYN = 8, FEAT_ORBIT = 16 };
+// (the default, MIXED_ORBIT): rays of a spherically symmetric metric
+// (Schwarzschild, Morris-Thorne) are turned into the frame of their own orbit
+// plane at load, stepped there on the equator, and turned back at the end;
+// FEAT_ORBIT_DYN: a per-ray flag says so (the serving kernel: camera rays).
+enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2, FEAT_PLANAR = 4, FEAT_PLANAR_DYN = 8, FEAT_ORBIT = 16,
+             FEAT_ORBIT_DYN = 32 };
 
 // Right-hand side on the equatorial plane: rhs_stage at sin theta = 1,
 // cos theta = 0, p^theta = 0, where its theta terms vanish (Gamma^th_phph =
@@ -92,8 +94,8 @@ __device__ __forceinline__ void rhs_planar(const AConsts<float>& C, float r, flo
   *k7 = (u * ir) * p3;
 }
 
-template <int K, int FEAT = 0>
-struct MixedStepper {
+template <int FEAT>
+struct MixedCore {
   float hi[8], lo[8];
   AConsts<float> C;
   float cap_hi, cap_lo, esc_hi, esc_lo;
@@ -102,11 +104,32 @@ struct MixedStepper {
   unsigned nsteps = 0;  // steps this ray has taken: renormalisation follows the ray, not the lane
   bool ready = false;
   bool planar = (FEAT & FEAT_PLANAR) != 0;
-  float oe1[3], oe2[3];  // orbit-plane frame (FEAT_ORBIT only)
+  bool orbit = (FEAT & FEAT_ORBIT) != 0;
+  float oe1[3], oe2[3];  // orbit-plane frame (FEAT_ORBIT, FEAT_ORBIT_DYN)
+  // rays of metric kind K can step in their orbit-plane frame
+  template <int K>
+  static constexpr bool any_orbit() {
+    return (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) && (FEAT & (FEAT_ORBIT | FEAT_ORBIT_DYN)) != 0;
+  }
 
-  // Serving: the source of the ray just loaded (equatorial rays step on the plane).
+  // Serving: the source of the ray about to be loaded or resumed (equatorial
+  // rays step on their plane, camera rays in their orbit plane).
   __device__ __forceinline__ void set_source(int src) {
     if (FEAT & FEAT_PLANAR_DYN) planar = src == SRC_EQUATORIAL;
+    if (FEAT & FEAT_ORBIT_DYN) orbit = src == SRC_CAMERA;
+  }
+  // Serving: a resumed camera ray gets its orbit-plane frame back from its
+  // initial state (the frame is a function of it, so it is the one the ray
+  // was loaded with).
+  template <int K>
+  __device__ __forceinline__ void resume_frame_k(const TraceLaunch& L, int64_t ray) {
+    if constexpr (any_orbit<K>()) {
+      if (orbit) {
+        double y0[8], yr[8];
+        camera_ray(L.cam, ray, y0);
+        orbit_in(y0, yr, oe1, oe2);
+      }
+    }
   }
 
   __device__ __forceinline__ void setup(const TraceLaunch& L) {
@@ -131,32 +154,39 @@ struct MixedStepper {
     }
   }
 
-  __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) {
+  template <int K>
+  __device__ __forceinline__ void load_k(const TraceLaunch& L, const double y0[8]) {
     if (!ready) setup(L);
     nsteps = 0;
-    if constexpr ((FEAT & FEAT_ORBIT) != 0) {
-      double yr[8];
-      orbit_in(y0, yr, oe1, oe2);
-      load_state(yr);
-    } else {
-      load_state(y0);
+    if constexpr (any_orbit<K>()) {
+      if (orbit) {
+        double yr[8];
+        orbit_in(y0, yr, oe1, oe2);
+        load_state(yr);
+        return;
+      }
     }
+    load_state(y0);
   }
 
-  __device__ __forceinline__ void to_double(double out[8]) const {
-    if constexpr ((FEAT & FEAT_ORBIT) != 0) {
-      double yr[8];
+  template <int K>
+  __device__ __forceinline__ void to_double_k(double out[8]) const {
+    double y[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) yr[i] = (double)hi[i] + (double)lo[i];
-      orbit_out(yr, oe1, oe2, out);
-    } else {
-#pragma unroll
-      for (int i = 0; i < 8; ++i) out[i] = (double)hi[i] + (double)lo[i];
+    for (int i = 0; i < 8; ++i) y[i] = (double)hi[i] + (double)lo[i];
+    if constexpr (any_orbit<K>()) {
+      if (orbit) {
+        orbit_out(y, oe1, oe2, out);
+        return;
+      }
     }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = y[i];
   }
 
   // Termination tests of the reference, evaluated on the compensated state.
-  __device__ __forceinline__ int terminate(const TraceLaunch&) const {
+  template <int K>
+  __device__ __forceinline__ int terminate_k(const TraceLaunch&) const {
     if (K == KIND_SCHWARZSCHILD) {
       if (!isfinite(hi[1])) return TERM_DIVERGED;
       // Far from both radii the high word decides: |lo| stays below 2^-20 of
@@ -177,12 +207,25 @@ struct MixedStepper {
     }
   }
 
+  // A Schwarzschild ray moving inward inside the photon sphere (r < 3M, p^r < 0)
+  // has no turning point left: it falls through the horizon. Near the horizon
+  // p^t = E/f grows without bound and the fixed step stops resolving it; a step
+  // whose p^t increment is a quarter of p^t or more (or not finite) is such a
+  // step, and its result would fling the ray off its geodesic (the reference
+  // then reports it Escaped at r ~ 1e30 or Diverged). The ray is reported
+  // Captured there instead. Elsewhere |increment / p^t| = 2 M h |p^r| / (r^2 f)
+  // stays far below a quarter at any sensible step.
+  __device__ __forceinline__ bool unresolved_infall(float inc_pt) const {
+    return hi[5] < 0.0f && hi[1] < 1.5f * C.two_m && !(fabsf(inc_pt) < 0.25f * hi[4]);
+  }
+
   // Returns STEP_OK, STEP_NONFINITE (state unchanged) or STEP_HORIZON: an RK4
   // stage of a Schwarzschild ray reached r <= 2M, where f = 1 - 2M/r changes
   // sign and the fixed step has no meaning; the ray has crossed the horizon and
   // is reported Captured. (The FP64 path keeps the reference's behaviour: such a
   // step overflows or throws the ray to r ~ 1e30, reported Diverged or Escaped.)
-  __device__ __forceinline__ int step_fp32(const TraceLaunch& L) {
+  template <int K>
+  __device__ __forceinline__ int step_fp32_k(const TraceLaunch& L) {
     float s0 = 0.0f, c0 = 1.0f;
     if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) sincosf(hi[2], &s0, &c0);
     float k[8], acc[8], p[4];
@@ -218,6 +261,7 @@ struct MixedStepper {
       inc[i] = sixth * (acc[i] + k[i]);
       finite &= isfinite(inc[i]);
     }
+    if (K == KIND_SCHWARZSCHILD && unresolved_infall(inc[4])) return STEP_HORIZON;
     if (!finite) return STEP_NONFINITE;
     // Positions move monotonically in t and phi and stay far from 0 in r and
     // theta relative to one step, so Fast2Sum is exact for them (and for t = 0 or
@@ -251,7 +295,8 @@ struct MixedStepper {
   // six components that move (t, r or l, phi and their momenta), theta and
   // p^theta held at their loaded values (pi/2 and 0). Same stage points,
   // horizon rule, compensated update and renormalisation as step_fp32.
-  __device__ __forceinline__ int step_fp32_planar(const TraceLaunch& L) {
+  template <int K>
+  __device__ __forceinline__ int step_fp32_planar_k(const TraceLaunch& L) {
     float k1, k4, k5, k7;
     float p0 = hi[4], p1 = hi[5], p3 = hi[7];
     rhs_planar<K>(C, hi[1], p0, p1, p3, &k4, &k5, &k7);
@@ -281,6 +326,7 @@ struct MixedStepper {
     if (K == KIND_SCHWARZSCHILD && !(rmin > C.two_m)) return STEP_HORIZON;
     const float i0 = sixth * (a0 + k0), i1 = sixth * (a1 + k1), i3 = sixth * (a3 + k3);
     const float i4 = sixth * (a4 + k4), i5 = sixth * (a5 + k5), i7 = sixth * (a7 + k7);
+    if (K == KIND_SCHWARZSCHILD && unresolved_infall(i4)) return STEP_HORIZON;
     // NaN guard on the momenta: every stage value of p^t, p^r, p^phi enters
     // k4, k5, k7 and so the momentum increments, so a non-finite t, r or phi
     // increment (sums of those stage values) implies a non-finite momentum
@@ -316,11 +362,12 @@ struct MixedStepper {
   }
 
   // FP64 RK4 with the closed-form right-hand side (band steps).
-  __device__ __forceinline__ int step_fp64(const TraceLaunch& L) {
+  template <int K>
+  __device__ __forceinline__ int step_fp64_k(const TraceLaunch& L) {
     AConsts<double> Cd;
     Cd.init(L.M);
     double y[8];
-    to_double(y);
+    to_double_k<K>(y);
     double s0 = 0.0, c0 = 1.0;
     if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) ::sincos(y[2], &s0, &c0);
     const double zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -361,13 +408,14 @@ struct MixedStepper {
     return STEP_OK;
   }
 
-  __device__ __forceinline__ int step(const TraceLaunch& L) {
+  template <int K>
+  __device__ __forceinline__ int step_k(const TraceLaunch& L) {
     if ((FEAT & FEAT_BAND) && K != KIND_MINKOWSKI && L.band > 0.0f && in_band<K>(L.M, hi[1], hi[2], hi[3], L.band))
-      return step_fp64(L);
-    if ((FEAT & FEAT_ORBIT) && (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE)) return step_fp32_planar(L);
+      return step_fp64_k<K>(L);
+    if (any_orbit<K>() && orbit) return step_fp32_planar_k<K>(L);
     if (K == KIND_SCHWARZSCHILD && (FEAT & (FEAT_PLANAR | FEAT_PLANAR_DYN)) && ((FEAT & FEAT_PLANAR) || planar))
-      return step_fp32_planar(L);
-    return step_fp32(L);
+      return step_fp32_planar_k<K>(L);
+    return step_fp32_k<K>(L);
   }
 
   __device__ __forceinline__ void finish(const TraceLaunch&) {}
@@ -388,6 +436,67 @@ struct MixedStepper {
     for (int i = 0; i < 8; ++i) {
       hi[i] = __uint_as_float(w[i]);
       lo[i] = __uint_as_float(w[8 + i]);
+    }
+  }
+};
+
+
+// The stepper of one metric kind K (every ray of the launch has that kind).
+template <int K, int FEAT = 0>
+struct MixedStepper : MixedCore<FEAT> {
+  __device__ __forceinline__ void resume_frame(const TraceLaunch& L, int64_t ray) {
+    this->template resume_frame_k<K>(L, ray);
+  }
+  __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) { this->template load_k<K>(L, y0); }
+  __device__ __forceinline__ void to_double(double out[8]) const { this->template to_double_k<K>(out); }
+  __device__ __forceinline__ int terminate(const TraceLaunch& L) const { return this->template terminate_k<K>(L); }
+  __device__ __forceinline__ int step(const TraceLaunch& L) { return this->template step_k<K>(L); }
+};
+
+// The stepper of a launch whose rays have different metric kinds (several
+// renders traced by one persistent kernel): each lane keeps the kind of the
+// ray it holds and branches on it; lanes of a warp mostly hold rays of one job,
+// claimed together, so the branch is mostly uniform.
+template <int FEAT>
+struct MixedStepperAny : MixedCore<FEAT> {
+  int kind = KIND_MINKOWSKI;
+  // A lane takes a ray of job L: its metric constants and kind.
+  __device__ __forceinline__ void bind(const TraceLaunch& L, int src) {
+    this->setup(L);
+    kind = L.M.kind;
+    this->orbit = (FEAT & FEAT_ORBIT_DYN) && src == SRC_CAMERA && (L.mixed_flags & MIXED_ORBIT) &&
+                  (kind == KIND_SCHWARZSCHILD || kind == KIND_MORRIS_THORNE);
+  }
+  __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) {
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: this->template load_k<KIND_SCHWARZSCHILD>(L, y0); return;
+      case KIND_MORRIS_THORNE: this->template load_k<KIND_MORRIS_THORNE>(L, y0); return;
+      case KIND_ALCUBIERRE: this->template load_k<KIND_ALCUBIERRE>(L, y0); return;
+      default: this->template load_k<KIND_MINKOWSKI>(L, y0); return;
+    }
+  }
+  __device__ __forceinline__ void to_double(double out[8]) const {
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: this->template to_double_k<KIND_SCHWARZSCHILD>(out); return;
+      case KIND_MORRIS_THORNE: this->template to_double_k<KIND_MORRIS_THORNE>(out); return;
+      case KIND_ALCUBIERRE: this->template to_double_k<KIND_ALCUBIERRE>(out); return;
+      default: this->template to_double_k<KIND_MINKOWSKI>(out); return;
+    }
+  }
+  __device__ __forceinline__ int terminate(const TraceLaunch& L) const {
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: return this->template terminate_k<KIND_SCHWARZSCHILD>(L);
+      case KIND_MORRIS_THORNE: return this->template terminate_k<KIND_MORRIS_THORNE>(L);
+      case KIND_ALCUBIERRE: return this->template terminate_k<KIND_ALCUBIERRE>(L);
+      default: return this->template terminate_k<KIND_MINKOWSKI>(L);
+    }
+  }
+  __device__ __forceinline__ int step(const TraceLaunch& L) {
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: return this->template step_k<KIND_SCHWARZSCHILD>(L);
+      case KIND_MORRIS_THORNE: return this->template step_k<KIND_MORRIS_THORNE>(L);
+      case KIND_ALCUBIERRE: return this->template step_k<KIND_ALCUBIERRE>(L);
+      default: return this->template step_k<KIND_MINKOWSKI>(L);
     }
   }
 };
@@ -426,10 +535,16 @@ template <int K, int SRC, int SINK>
 static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
   const int feat = ((K != KIND_MINKOWSKI && L.band > 0.0f) ? FEAT_BAND : 0) |
                    ((L.mixed_flags & MIXED_REPROJECT) ? FEAT_REPROJECT : 0);
-  if constexpr ((K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) && SRC == SRC_CAMERA && SINK == SINK_RENDER) {
-    // orbit-plane frame (opt-in): renders only, whose sink needs the escape
-    // direction, not the unwrapped final phi
-    if (feat == 0 && (L.mixed_flags & MIXED_ORBIT)) return launch_mst_v<K, SRC, SINK, 1, FEAT_ORBIT>(L, s);
+  if constexpr ((K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) && SRC != SRC_EQUATORIAL) {
+    // orbit-plane frame (the default for camera rays and ray arrays of the
+    // spherically symmetric metrics; equatorial rays already step on their plane)
+    if (feat == 0 && (L.mixed_flags & MIXED_ORBIT)) {
+      switch (L.variant) {
+        case 1: return launch_mst_v<K, SRC, SINK, 8, FEAT_ORBIT>(L, s);
+        case 2: return launch_mst_v<K, SRC, SINK, 10, FEAT_ORBIT>(L, s);
+        default: return launch_mst_v<K, SRC, SINK, 1, FEAT_ORBIT>(L, s);
+      }
+    }
   }
   switch (feat) {  // the optional parts run without a register cap
     case FEAT_BAND: return launch_mst_v<K, SRC, SINK, 1, FEAT_BAND>(L, s);
@@ -443,13 +558,42 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
   }
 }
 
+// One persistent kernel over the rays of several renders (any metric kinds):
+// the default mixed step per ray, camera rays of the spherically symmetric
+// metrics in their orbit plane when the orbit-plane option is on (as in the
+// single-render kernels, so each image equals its single render).
+__global__ void __launch_bounds__(TRACE_BLOCK) trace_multi_mixed_kernel(const TraceLaunch* jobs, const MultiDesc D) {
+  trace_loop_multi<MixedStepperAny<FEAT_ORBIT_DYN>, SRC_CAMERA, SINK_RENDER>(jobs, D);
+}
+
+cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s) {
+  static int sms = 0, per_sm = 0;
+  if (sms == 0) {
+    int dev = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_multi_mixed_kernel, TRACE_BLOCK, 0);
+    per_sm = occ < 1 ? 1 : occ;
+  }
+  const int64_t n = D.start[D.njobs];
+  if (n <= 0) return cudaSuccess;
+  const int64_t slots = persistent_slots(sms, per_sm, reserve);
+  const int64_t need = (n + TRACE_BLOCK - 1) / TRACE_BLOCK;
+  const int grid = (int)(need < slots ? need : slots);
+  trace_multi_mixed_kernel<<<grid < 1 ? 1 : grid, TRACE_BLOCK, 0, s>>>(jobs, D);
+  return cudaGetLastError();
+}
+
 // Serving engine kernel for the mixed-precision classes (serve_common.cuh),
 // no register cap. The server runs the default mixed step (no FP64 band, no
-// re-projection).
+// re-projection; camera rays of the spherically symmetric metrics in their
+// orbit plane, equatorial rays on theirs), as the single calls do by default.
 template <int K>
 __global__ void __launch_bounds__(TRACE_BLOCK, 7) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
                                                                      ServeClass* cl, const unsigned* epoch, int budget) {
-  serve_loop<MixedStepper<K, K == KIND_SCHWARZSCHILD ? FEAT_PLANAR_DYN : 0>, K>(jobs, cnt, cl, epoch, budget);
+  constexpr int F = K == KIND_SCHWARZSCHILD ? (FEAT_PLANAR_DYN | FEAT_ORBIT_DYN)
+                    : K == KIND_MORRIS_THORNE ? FEAT_ORBIT_DYN : 0;
+  serve_loop<MixedStepper<K, F>, K>(jobs, cnt, cl, epoch, budget);
 }
 
 int serve_mixed_blocks_per_sm(int kind) {

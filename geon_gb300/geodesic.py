@@ -6,8 +6,9 @@ import numpy as np
 from . import _ffi
 from ._util import check, dp, f64, i32p, i64p, points
 
-FP64, MIXED, ADAPTIVE = 0, 1, 2
-PRECISION = {"fp64": FP64, "mixed": MIXED, "adaptive": ADAPTIVE, FP64: FP64, MIXED: MIXED, ADAPTIVE: ADAPTIVE}
+FP64, MIXED, ADAPTIVE, FP64_FAST = 0, 1, 2, 3
+PRECISION = {"fp64": FP64, "mixed": MIXED, "adaptive": ADAPTIVE, "fp64fast": FP64_FAST,
+             FP64: FP64, MIXED: MIXED, ADAPTIVE: ADAPTIVE, FP64_FAST: FP64_FAST}
 
 
 def set_adaptive_tolerance(rtol, atol):

@@ -62,6 +62,33 @@ def render(metric, camera, cfg=None, with_classes=False):
     return rgb, stats
 
 
+def render_batch(items):
+    """Several renders traced by one persistent kernel launch (geon_render_batch):
+    items is a list of (metric, camera, cfg); every cfg has the same precision.
+    Returns a list of (pixels, RenderStats, class map, steps map), each equal to
+    render(metric, camera, cfg, with_classes=True) of that item alone."""
+    n = len(items)
+    arr = (_ffi.GeonRenderItem * n)()
+    outs = []
+    for j, (metric, camera, cfg) in enumerate(items):
+        cfg = cfg or RenderConfig()
+        rgb = np.empty((camera.height, camera.width, 3), dtype=np.float32)
+        cls = np.empty((camera.height, camera.width), dtype=np.int32)
+        pst = np.empty((camera.height, camera.width), dtype=np.int64)
+        st = _ffi.GeonRenderStats()
+        arr[j].metric = metric.handle.value
+        arr[j].camera = camera.c_struct()
+        arr[j].render = cfg.c_struct()
+        arr[j].rgb = rgb.ctypes.data
+        arr[j].stats = _ffi.ctypes.pointer(st)
+        arr[j].pixel_class = cls.ctypes.data
+        arr[j].pixel_steps = pst.ctypes.data
+        outs.append((rgb, st, cls, pst))
+    check(_ffi.load().geon_render_batch(arr, n))
+    return [(rgb, RenderStats(st.captured, st.escaped, st.diverged, st.max_null_residual, st.avg_steps,
+                              st.total_steps), cls, pst) for rgb, st, cls, pst in outs]
+
+
 def render_u8(metric, camera, cfg=None, with_float=False):
     """render() followed by write_png's tonemap on the GPU: (height, width, 3)
     uint8, the bytes write_png encodes [+ the float image], and RenderStats."""

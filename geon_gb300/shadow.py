@@ -4,7 +4,7 @@ import numpy as np
 
 from . import _ffi
 from ._util import check, dp, f64, i32p, i64p
-from .geodesic import PRECISION
+from .geodesic import PRECISION, TraceResult
 from .metric import CAPTURED
 
 
@@ -23,6 +23,20 @@ def classify(metric, r_obs, alpha, step=0.01, max_steps=200000, precision="fp64"
     check(_ffi.load().geon_shadow_classify(metric.handle, float(r_obs), dp(a), a.size, float(step),
                                            int(max_steps), PRECISION[precision], i32p(term), i64p(steps)))
     return term, steps
+
+
+def trace(metric, r_obs, alpha, step=0.01, max_steps=200000, precision="fp64"):
+    """geodesic::trace of the equatorial ray at each launch angle, with the
+    stepper classify() uses for them; a TraceResult per ray."""
+    a = f64(np.atleast_1d(alpha))
+    n = a.size
+    term = np.empty(n, dtype=np.int32)
+    yf = np.empty((n, 8))
+    steps = np.empty(n, dtype=np.int64)
+    resid = np.empty(n)
+    check(_ffi.load().geon_shadow_trace(metric.handle, float(r_obs), dp(a), n, float(step), int(max_steps),
+                                        PRECISION[precision], i32p(term), dp(yf), i64p(steps), dp(resid)))
+    return TraceResult(term, yf, steps, resid)
 
 
 def is_captured(metric, r_obs, alpha, step=0.01, max_steps=200000, precision="fp64"):
@@ -48,27 +62,3 @@ def impact_parameter(metric, r_obs, alpha):
     """b = r_obs sin(alpha) / sqrt(1 - 2M/r_obs) (bin/validate_shadow.rs:78-79)."""
     f = 1.0 - 2.0 * metric.mass / r_obs
     return r_obs * np.sin(alpha) / np.sqrt(f)
-
-
-def physical_class(metric, result, max_steps):
-    """Map the reference's numerical accidents at the horizon to Captured.
-
-    With the reference's fixed RK4 step, a ray whose step straddles r = 2M
-    evaluates the Christoffel symbols where f = 1 - 2M/r is ~0; the step then
-    either overflows (the NaN guard reports Diverged, geodesic.rs:89-100) or
-    throws the ray to a state far off the null cone, often at an absurd radius
-    that the next check reports as Escaped. All of these are captures. Returns a
-    copy of result.termination with such rays set to Captured: Diverged before
-    the step cap, and Escaped with r > 2 * escape radius (a real escape ends
-    within one step of it) or |g(p, p)| > 1e-6 (p^t)^2.
-    """
-    term = np.array(result.termination, copy=True)
-    y = np.asarray(result.final_state)
-    r = y[:, 1]
-    steps = np.asarray(result.steps_taken)
-    resid = np.asarray(result.null_residual)
-    off_cone = ~(resid <= 1e-6 * np.maximum(1.0, y[:, 4] ** 2))
-    flung = (term == 2) & (~(r <= 2.0 * metric.escape_radius * metric.mass) | off_cone)
-    nan_fall = (term == 0) & (steps < max_steps)
-    term[flung | nan_fall] = CAPTURED
-    return term

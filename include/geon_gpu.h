@@ -4,8 +4,8 @@
  * A drop-in for the hot path of the geon crate (Rust): the Metric trait's
  * functors with their finite-difference fallbacks, geodesic::trace, the Camera
  * tetrad, render(), the shadow bisection of bin/validate_shadow.rs and the
- * curvature.rs chain. A Rust host binds these with `extern "C"` declarations
- * (INTEGRATION.md shows the shim); every array layout below is the memory layout
+ * curvature.rs chain. A Rust host binds these with `extern "C"` declarations;
+ * every array layout below is the memory layout
  * of the corresponding Rust type, so slices pass through without copies:
  *   Vec4 = [f64; 4], Mat4 = [[f64; 4]; 4] (row-major), Christoffel =
  *   [[[f64; 4]; 4]; 4] indexed [mu][alpha][beta], State = [f64; 8] =
@@ -66,7 +66,14 @@ enum geon_termination { GEON_DIVERGED = 0, GEON_CAPTURED = 1, GEON_ESCAPED = 2 }
  * integrator.rs:5-7): FP64 Dormand-Prince 5(4) with error control instead of
  * the fixed-step RK4; `step` is the first trial step, max_steps caps accepted
  * steps, tolerances from geon_set_adaptive_tolerance. Not for the server. */
-enum geon_precision { GEON_FP64 = 0, GEON_MIXED = 1, GEON_ADAPTIVE = 2 };
+/* GEON_FP64_FAST (an extension): FP64 fixed-step RK4 in the same chart, with the
+ * same stage points, termination tests, NaN guard and step cap as GEON_FP64,
+ * held to the reference CUDA kernel's tolerance (cuda/schwarzschild_render.cu:3-5,
+ * equal "up to associativity") instead of to the reference's bits: fused
+ * multiply-adds, one reciprocal per right-hand side, sin/cos of the polar angle
+ * once per step. Schwarzschild only; other metrics run the GEON_FP64 stepper.
+ * Not for the server. */
+enum geon_precision { GEON_FP64 = 0, GEON_MIXED = 1, GEON_ADAPTIVE = 2, GEON_FP64_FAST = 3 };
 
 typedef struct geon_metric* geon_metric_t;
 
@@ -187,6 +194,23 @@ int geon_render_ex(geon_metric_t m, const geon_camera* cam, const geon_render_co
  * rgb (the f32 image) may be NULL. */
 int geon_render_u8(geon_metric_t m, const geon_camera* cam, const geon_render_config* cfg,
                    uint8_t* rgb8, float* rgb, geon_render_stats* stats);
+/* Several renders traced together by ONE persistent kernel launch: the rays of
+ * every item share one device work queue, and a lane that finishes a ray takes
+ * the next one of any item (any metric kind), so images of uneven path length
+ * keep the GPU full until the last ray. Each item's outputs equal what
+ * geon_render_ex gives for it alone, bit for bit. 1 to 8 items, one precision
+ * for all (GEON_FP64 or GEON_MIXED); sampled metrics are not supported. An
+ * extension: the reference renders one image per call (render.rs:55-166). */
+typedef struct {
+  geon_metric_t metric;
+  geon_camera camera;
+  geon_render_config render;
+  float* rgb;                 /* out: width*height*3 */
+  geon_render_stats* stats;   /* out, may be NULL */
+  int32_t* pixel_class;       /* out, may be NULL */
+  int64_t* pixel_steps;       /* out, may be NULL */
+} geon_render_item;
+int geon_render_batch(const geon_render_item* items, size_t n);
 /* write_png's tonemap (render.rs:174-178) alone, over n floats. */
 int geon_tonemap_u8(const float* rgb, size_t n, uint8_t* out);
 int geon_tonemap_u8_dev(const float* rgb, size_t n, uint8_t* out, void* stream);
@@ -205,12 +229,17 @@ int geon_get_show_stars(void);
 int geon_set_mixed_band(int kind, double band);
 double geon_get_mixed_band(int kind);
 void geon_set_mixed_reproject(int on);
-/* Opt-in (default off): mixed-precision renders of the spherically symmetric
- * metrics (Schwarzschild, Morris-Thorne) trace each camera ray in the frame of
- * its own orbit plane, on the equator with no trigonometry in the step, and
- * turn its final state back for the sky lookup. Same geodesics; not the
- * default mixed step's bits. Renders only (the frame does not count turns of
- * phi); not applied to served requests. No counterpart in the reference. */
+/* Default on: GEON_MIXED traces of the spherically symmetric metrics
+ * (Schwarzschild, Morris-Thorne), camera rays and ray arrays, step each ray in
+ * the frame of its own orbit plane, on the equator with no trigonometry in the
+ * step, and turn its final state back into the chart; every geodesic of these
+ * metrics lies in a plane through the centre, so the frame is exact geometry
+ * and keeps the rays away from the chart's polar axis, where the reference's
+ * (theta, phi) step flings rays off their geodesic. The final state is the same
+ * point of the geodesic with theta in [0, pi] and phi in (-pi, pi] (the frame
+ * does not count turns of phi). Served camera rays use it too. Off (0): the
+ * rays step in the chart (the FP64 band and null re-projection options step
+ * in the chart whatever this says). No counterpart in the reference. */
 void geon_set_mixed_orbit_plane(int on);
 int geon_get_mixed_orbit_plane(void);
 /* Error tolerances of GEON_ADAPTIVE: a step is accepted when
@@ -292,6 +321,14 @@ int geon_equatorial_rays(geon_metric_t schwarzschild, double r_obs, const double
 int geon_shadow_classify(geon_metric_t schwarzschild, double r_obs, const double* alpha, size_t n,
                          double step, int64_t max_steps, int precision, int32_t* term,
                          int64_t* steps);
+/* geodesic::trace (geodesic.rs:62-117) of the equatorial rays of n launch angles
+ * (validate_shadow.rs:20-35), with the stepper geon_shadow_classify uses for
+ * them (the mixed path steps them on their invariant plane). Outputs as
+ * geon_trace; final_state, steps and null_residual may be NULL. An extension:
+ * the reference traces these rays only inside is_captured. */
+int geon_shadow_trace(geon_metric_t schwarzschild, double r_obs, const double* alpha, size_t n,
+                      double step, int64_t max_steps, int precision, int32_t* term,
+                      double* final_state, int64_t* steps, double* null_residual);
 /* nb independent bisections of `iters` halvings each on [lo[i], hi[i]]
  * (bin/validate_shadow.rs:70-79). Outputs alpha_c = 0.5*(lo+hi) after the loop;
  * lo_out/hi_out/steps_out (ray-steps spent) may be NULL. With GEON_FP64 the
@@ -316,12 +353,16 @@ int geon_shadow_bisect_dev(geon_metric_t schwarzschild, double r_obs, const doub
  * memory while they run (a host that owns all device memory through its own
  * pool, a real-time loop with no room for an allocator call, code that must not
  * fail with "out of memory" mid-way). Its working memory is one fixed 512 KiB
- * array compiled into the library, held on every GPU that loads the library
- * until exit; at most 4096 brackets per call (larger: GEON_ERR_INVALID). The
- * first call on each device looks up that array's device address; make it
- * before any stream capture. Calls share the array: calls that overlap on the
- * GPU race with each other, so order them on one stream. Same arguments and
- * results as geon_shadow_bisect_dev. */
+ * array compiled into the library; at most 4096 brackets per call (larger:
+ * GEON_ERR_INVALID). Every call looks up the array's device address on the
+ * current device. With CUDA's lazy module loading, the array and the kernels'
+ * code are placed on a device at their first use there, so the first call on
+ * each device takes that memory (once; it is held until exit): make the first
+ * call before the caller reserves the rest of the device memory, and before any
+ * stream capture. Calls share the array: calls that overlap on the GPU race
+ * with each other, so order them on one stream. The speculative width is the
+ * default one (geon_set_bisect_rays_per_round does not apply). Same arguments
+ * and results as geon_shadow_bisect_dev. */
 int geon_shadow_bisect_dev_noalloc(geon_metric_t schwarzschild, double r_obs, const double* lo,
                                    const double* hi, size_t nb, int iters, double step,
                                    int64_t max_steps, int precision, double* alpha_c,
@@ -338,8 +379,9 @@ int geon_shadow_bisect_dev_noalloc(geon_metric_t schwarzschild, double r_obs, co
  * Each result is the one the matching single-call entry point gives
  * (geon_render_ex, geon_shadow_bisect with one bracket, geon_curvature_grid),
  * bit for bit, whatever else runs beside it. Mixed-precision requests run the
- * default mixed step (geon_set_mixed_band / geon_set_mixed_reproject /
- * geon_set_mixed_orbit_plane are not applied to served requests). */
+ * default mixed step (camera rays of Schwarzschild and Morris-Thorne in their
+ * orbit plane); geon_set_mixed_band, geon_set_mixed_reproject and
+ * geon_set_mixed_orbit_plane(0) are not applied to served requests. */
 typedef struct geon_server* geon_server_t;
 enum geon_job_type { GEON_JOB_RENDER = 0, GEON_JOB_BISECT = 1, GEON_JOB_CURVATURE = 2 };
 

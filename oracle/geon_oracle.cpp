@@ -47,6 +47,14 @@ enum { DIVERGED = 0, CAPTURED = 1, ESCAPED = 2, NONE = -1 };
 // The sin/cos constants are the double roundings of pi/2, 2/pi and 1/n!,
 // derived with mpmath by geon_gb300/csrc/gen_math_constants.py; the expm1
 // constants are the published ones.
+//
+// The expm1/tanh method, its range thresholds and its constants follow fdlibm,
+// whose notice is kept here as its licence asks:
+//   Copyright (C) 1993 by Sun Microsystems, Inc. All rights reserved.
+//   Developed at SunSoft, a Sun Microsystems, Inc. business.
+//   Permission to use, copy, modify, and distribute this
+//   software is freely granted, provided that this notice
+//   is preserved.
 // ---------------------------------------------------------------------------
 constexpr double GM_PIO2_1 = 0x1.921fb54442d18p+0;
 constexpr double GM_PIO2_2 = 0x1.1a62633145c07p-54;

@@ -16,7 +16,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(OUT, "schwarzschild_render.cubin")
-REFERENCE = os.environ.get("GEON_REFERENCE_DIR", "/root/reference")
+# the reference checkout: GEON_REFERENCE_DIR, else a checkout named "reference"
+# beside this repository
+REFERENCE = os.environ.get("GEON_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 SRC = os.path.join(REFERENCE, "cuda", "schwarzschild_render.cu")
 # the kernel's mangled name: trace_kernel(int, int, double, double, double,
 # double, int, double, double, int*, double*)

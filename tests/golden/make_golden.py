@@ -5,16 +5,20 @@ Reads, as text, the known-answer output the reference commits
 as parsed values and line for line) and the
 shadow-validation lines of its README (README.md:43-45, the stdout of
 bin/validate_shadow.rs), and writes them as JSON next to this script. Run in a
-checkout where the reference sits at REFERENCE (default /root/reference); the
-JSON files are committed so the tests never need the reference itself.
+checkout where the reference sits at GEON_REFERENCE_DIR (default: a checkout
+named "reference" beside this repository); the JSON files are committed so the
+tests never need the reference itself.
 """
 import json
 import os
 import re
 import sys
 
-REF = os.environ.get("REFERENCE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference checkout: GEON_REFERENCE_DIR, else a checkout named "reference"
+# beside this repository
+REF = os.environ.get("GEON_REFERENCE_DIR") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference")
 NUM = r"[+-]?\d+\.\d+e[+-]?\d+"
 
 

@@ -78,7 +78,8 @@ def test_struct_layouts_match_header(tmp_path):
         pytest.skip("no C compiler")
     structs = {"geon_camera": _ffi.GeonCamera, "geon_render_config": _ffi.GeonRenderConfig,
                "geon_render_stats": _ffi.GeonRenderStats, "geon_grid": _ffi.GeonGrid,
-               "geon_job": _ffi.GeonJob, "geon_server_stats": _ffi.GeonServerStats}
+               "geon_job": _ffi.GeonJob, "geon_server_stats": _ffi.GeonServerStats,
+               "geon_render_item": _ffi.GeonRenderItem}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "geon_gpu.h"', "int main(void) {"]
     expect = []
     for cname, cls in structs.items():
@@ -127,12 +128,22 @@ def test_server_tuning_argument_errors_without_gpu(lib):
     assert lib.geon_server_autotune(None, None, None) == -1
 
 
+def test_render_batch_argument_errors_without_gpu(lib):
+    from geon_gb300 import _ffi
+    assert lib.geon_render_batch(None, 0) == 0  # nothing to do
+    items = (_ffi.GeonRenderItem * 9)()
+    assert lib.geon_render_batch(items, 9) == -1  # at most 8 items
+    assert b"1 to 8" in lib.geon_last_error()
+    items[0].render.precision = 2  # the adaptive stepper has no batched kernel
+    assert lib.geon_render_batch(items, 1) == -1
+
+
 def test_mixed_orbit_plane_flag_without_gpu(lib):
-    assert lib.geon_get_mixed_orbit_plane() == 0  # off by default
-    lib.geon_set_mixed_orbit_plane(1)
-    assert lib.geon_get_mixed_orbit_plane() == 1
+    assert lib.geon_get_mixed_orbit_plane() == 1  # on by default
     lib.geon_set_mixed_orbit_plane(0)
     assert lib.geon_get_mixed_orbit_plane() == 0
+    lib.geon_set_mixed_orbit_plane(1)
+    assert lib.geon_get_mixed_orbit_plane() == 1
 
 
 def test_persistent_reserve_setters_without_gpu(lib):

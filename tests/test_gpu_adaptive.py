@@ -61,8 +61,12 @@ def test_adaptive_classification_and_b_c(geon):
     y0 = geon.shadow.equatorial_ray(m, 20.0, alpha)
     fixed = geon.trace(m, y0, 0.01, 200000, precision="fp64")
     ad = geon.trace(m, y0, 0.01, 200000, precision="adaptive")
-    phys = geon.shadow.physical_class(m, fixed, 200000)
-    bad = np.where(phys != ad.termination)[0]
+    # where the adaptive and fixed-step classes differ, the independent FP64
+    # arbiter sides with the adaptive integration (the fixed step's horizon
+    # accidents), except for rays within 0.01 deg of the critical angle
+    dis = np.flatnonzero(fixed.termination != ad.termination)
+    arb = geon.accuracy.arbiter_classes(m, y0[dis], 0.01, 200000)
+    bad = dis[arb != ad.termination[dis]]
     assert np.all(np.abs(np.degrees(alpha[bad]) - 14.269) < 1e-2)
     assert ad.steps_taken.sum() * 50 < fixed.steps_taken.sum()
     ac, _, _, _ = geon.shadow.bisect(m, 20.0, 0.0, np.pi / 2 - 1e-3, iters=60, precision="adaptive")
