@@ -88,6 +88,13 @@ def workload_r30(seed):
     return alpha, lo, hi
 
 
+def shard_totals(dist, t_local, units_local, device="cpu"):
+    """The job's (time, units) over ranks: the slowest rank's time, the sum of
+    their units (geon_gb300.shard.job_totals)."""
+    from geon_gb300 import shard
+    return shard.job_totals(dist, t_local, units_local, device)
+
+
 def rank_workload(rank, seed=0x5EED):
     """The headline workload of one rank: its own seeded sweep and brackets."""
     from geon_gb300 import shard
@@ -335,7 +342,7 @@ def main():
     launches = lib.geon_launch_count() - launches0
     clocks = sampler.stop()
     times = [r["ms"] for r in res]
-    t_total, total_steps = shard.job_totals(dist, sum(times) / 1e3, sum(r["steps"] for r in res), dev)
+    t_total, total_steps = shard_totals(dist, sum(times) / 1e3, sum(r["steps"] for r in res), dev)
     value = total_steps / t_total
     sweep_steps = res[-1]["sweep_steps"]
     ac_run = run.d_ac.cpu().numpy()
@@ -399,6 +406,7 @@ def main():
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards",
                    "sweep_reserve_blocks_per_sm": args.reserve, "bisect_rays_per_round": args.bisect_rays,
                    "mixed_kernel_variant": None if tuned is None else tuned["variant"][1],
+                   "mixed_block_size": None if tuned is None else tuned.get("block_size", {}).get("equatorial"),
                    "autotune_rates": None if tuned is None else tuned.get("rates")},
         "latency": {"step_ms_p50": pct(times, 50), "step_ms_p99": pct(times, 99),
                     "bisection_ms_p50": pct([r["bisection_ms"] for r in res], 50),
@@ -926,17 +934,23 @@ def serve_requests(n, rate, seed):
     return reqs
 
 
-def run_serve_stream(geon, reqs, precision, budget):
-    """Submit the stream at its arrival times; returns the server's statistics."""
+def run_serve_stream(geon, reqs, precision, budget, window_s=None):
+    """Submit the stream at its arrival times. With window_s, requests stop
+    arriving at window_s and whatever is still queued or running then is
+    cancelled (its rays finished so far still count as integrated work); the
+    latencies of those requests are censored at the window. Returns the
+    server's statistics and the per-request outcome."""
     metrics = {0: geon.Minkowski(), 1: geon.Schwarzschild(1.0, 1.001, 100.0),
                2: geon.Alcubierre(2.0, 0.125, 0.5, 0.0), 3: geon.MorrisThorne(1.0)}
     sch = geon.Schwarzschild(1.0)
     grids = {0: ((-10.0, -10.0, -10.0), (10.0, 10.0, 10.0)), 1: ((3.0, 0.3, 0.0), (10.0, 2.8, 6.0)),
              2: ((-4.0, -4.0, -4.0), (4.0, 4.0, 4.0)), 3: ((-5.0, 0.3, 0.0), (5.0, 2.8, 6.0))}
-    jobs = []
+    jobs, t_sub = [], []
     with geon.Server(budget) as srv:
         t0 = time.perf_counter()
         for q in reqs:
+            if window_s is not None and q[1] >= window_s:
+                break
             wait = q[1] - (time.perf_counter() - t0)
             if wait > 0:
                 time.sleep(wait)
@@ -958,19 +972,62 @@ def run_serve_stream(geon, reqs, precision, budget):
                 lo, hi = grids[q[2]]
                 jobs.append(srv.submit_curvature(metrics[q[2]], lo, hi, (32, 32, 32), nk=16, seed=q[3],
                                                  with_einstein=True))
+            t_sub.append(time.perf_counter() - t0)
         t_submitted = time.perf_counter() - t0
+        cancelled = 0
+        if window_s is not None:
+            rest = window_s - (time.perf_counter() - t0)
+            if rest > 0:
+                try:
+                    srv.wait_all(timeout=rest)
+                except TimeoutError:
+                    pass
+            t_window = time.perf_counter() - t0
+            for j in jobs:
+                if j.poll() in (0, 1):
+                    j.cancel()
+                    cancelled += 1
         srv.wait_all()
         t_all = time.perf_counter() - t0
         st = srv.stats()
-        failed = [j.id for j in jobs if j.poll() != 2]
+        states = [j.poll() for j in jobs]
+    st["requests"] = len(jobs)
+    st["cancelled_at_window"] = cancelled
     st["submit_wall_s"] = t_submitted
     st["drain_wall_s"] = t_all
-    st["failed_ids"] = failed[:10]
+    st["window_s"] = window_s
+    if window_s is not None:
+        # requests unfinished at the window end: their latency is at least
+        # (window end - arrival); reported beside the completed ones' percentiles
+        cens = [1e3 * (t_window - t) for t, s_ in zip(t_sub, states) if s_ != 2]
+        st["censored_latencies"] = len(cens)
+        st["censored_latency_min_ms"] = min(cens) if cens else None
+        st["censored_latency_p50_ms"] = float(np.median(cens)) if cens else None
+        st["t_window_s"] = t_window
+    st["failed_ids"] = [j.id for j, s_ in zip(jobs, states) if s_ != 2][:10]
     return st
 
 
+def serve_summary(st, n_offered_s):
+    """Per-precision figures of one served run."""
+    wall = st["drain_wall_s"]
+    steps = st["ray_steps"] + st.get("ray_steps_unfinished", 0.0)
+    return {"ray_steps_per_s": steps / wall, "ray_steps_completed_per_s": st["ray_steps"] / wall,
+            "grid_points_per_s": st["grid_points"] / wall,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "by_type": st["by_type"],
+            "requests": st["requests"], "completed": st["completed"], "failed": st["failed"],
+            "cancelled_at_window": st["cancelled_at_window"],
+            "unfinished_latency_lower_bound_min_ms": st.get("censored_latency_min_ms"),
+            "unfinished_latency_lower_bound_p50_ms": st.get("censored_latency_p50_ms"),
+            "offered_requests_per_s": st["requests"] / n_offered_s,
+            "sustained_requests_per_s": st["completed"] / wall,
+            "wall_s": wall, "window_s": st["window_s"], "launches": st["launches"]}
+
+
 def serve_main(args):
-    """The serving stream, mixed then FP64, as one JSON line."""
+    """The serving stream for each precision (the same seeded requests) as one
+    JSON line; --rates adds a sweep of arrival rates (mixed) that locates the
+    saturation rate: the highest offered rate the server sustains."""
     import torch
     torch.cuda.set_device(0)
     import geon_gb300 as geon
@@ -979,40 +1036,46 @@ def serve_main(args):
                         geon.MorrisThorne(1.0), geon.Minkowski()):
         geon.autotune.autotune(kind_metric)
     reqs = serve_requests(args.requests, args.rate, 0x5E4E)
+    window = args.window if args.window > 0 else None
     sampler = ClockSampler(0)
     sampler.start()
     launches0 = lib.geon_launch_count()
-    legs = {}
+    out = {}
     for prec in args.serve_precisions.split(","):
-        legs[prec] = run_serve_stream(geon, reqs, prec, args.budget_gb << 30)
-        print(f"serving leg {prec}: " + json.dumps(legs[prec]), file=sys.stderr, flush=True)
+        st = run_serve_stream(geon, reqs, prec, args.budget_gb << 30, window)
+        offered_s = min(reqs[st["requests"] - 1][1], window or 1e30) if st["requests"] else 1.0
+        out[prec] = serve_summary(st, max(offered_s, 1e-3))
+        print(f"serving leg {prec}: " + json.dumps(out[prec]), file=sys.stderr, flush=True)
+    sweep = []
+    for rate in [float(r) for r in args.rates.split(",") if r]:
+        rq = serve_requests(max(4, int(rate * args.sweep_window)), rate, 0x5E4E + int(rate * 1000))
+        st = run_serve_stream(geon, rq, "mixed", args.budget_gb << 30, args.sweep_window)
+        sm = serve_summary(st, args.sweep_window)
+        sm["rate"] = rate
+        sweep.append(sm)
+        print(f"saturation sweep {rate}/s: " + json.dumps(sm), file=sys.stderr, flush=True)
     launches = lib.geon_launch_count() - launches0
     clocks = sampler.stop()
     n_types = {k: sum(1 for q in reqs if q[0] == k) for k in ("render", "bisect", "curvature")}
-    offered_s = reqs[-1][1]
-    out = {}
-    for prec, st in legs.items():
-        out[prec] = {"ray_steps_per_s": st["ray_steps"] / st["drain_wall_s"],
-                     "grid_points_per_s": st["grid_points"] / st["drain_wall_s"],
-                     "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "by_type": st["by_type"],
-                     "completed": st["completed"], "failed": st["failed"],
-                     "offered_requests_per_s": len(reqs) / offered_s,
-                     "sustained_requests_per_s": st["completed"] / st["drain_wall_s"],
-                     "drain_wall_s": st["drain_wall_s"], "launches": st["launches"]}
     main_prec = args.serve_precisions.split(",")[0]
     line = {"metric": "ray-steps/s", "value": out[main_prec]["ray_steps_per_s"], "unit": "ray-steps/s",
-            "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * legs[main_prec]["drain_wall_s"],
+            "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * out[main_prec]["wall_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (mixed: FP32 right-hand side, compensated f32-pair state)" if main_prec == "mixed" else "f64",
             "data": "synthetic seeded request stream",
-            "config": {"workload": f"serving stream: {len(reqs)} requests, Poisson mean {args.rate}/s "
-                                   f"({n_types['render']} renders 128^2-2048^2 over 4 metrics, "
+            "config": {"workload": f"serving stream: first {len(reqs)} requests of a Poisson stream, mean "
+                                   f"{args.rate}/s ({n_types['render']} renders 128^2-2048^2 over 4 metrics, "
                                    f"{n_types['bisect']} 32-halving bisections, {n_types['curvature']} "
                                    f"32^3 curvature slabs)", "budget_gb": args.budget_gb,
-                       "timing": "host wall clock, first submission to last completion"},
+                       "window_s": window,
+                       "timing": "host wall clock, first submission to the last request's end"},
             "serving": out, "gpu_launches": int(launches), "clocks": clocks}
     if "mixed" in out and "fp64" in out:
         line["serving"]["mixed_over_fp64_ray_steps"] = out["mixed"]["ray_steps_per_s"] / out["fp64"]["ray_steps_per_s"]
+    if sweep:
+        ok = [s_ for s_ in sweep if s_["cancelled_at_window"] == 0 and s_["failed"] == 0]
+        line["serving"]["saturation_sweep"] = sweep
+        line["serving"]["saturation_rate_requests_per_s"] = max((s_["rate"] for s_ in ok), default=None)
     print(json.dumps(line), flush=True)
 
 
@@ -1025,6 +1088,10 @@ if __name__ == "__main__":
         ap.add_argument("--budget-gb", type=int, default=64)
         ap.add_argument("--serve-precisions", default="mixed",
                         help="comma list; the fp64 stream of 200 requests runs for tens of minutes")
+        ap.add_argument("--window", type=float, default=0.0,
+                        help="serve: stop arrivals and cancel what is left after this many seconds (0: drain)")
+        ap.add_argument("--rates", default="", help="serve: comma list of arrival rates (mixed) to sweep")
+        ap.add_argument("--sweep-window", type=float, default=30.0, help="serve: seconds per swept rate")
         ap.add_argument("--size", type=int, default=2048, help="exotic: image side")
         ap.add_argument("--row-step", type=int, default=16, help="exotic: FP64 traces every k-th row")
         ap.add_argument("--grid", type=int, default=128, help="curvature: grid side")

@@ -83,7 +83,7 @@ class GeonServerStats(ctypes.Structure):
                 ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
                 ("p50_ms_by_type", ctypes.c_double * 3), ("p99_ms_by_type", ctypes.c_double * 3),
                 ("ray_steps", ctypes.c_double), ("grid_points", ctypes.c_double), ("wall_s", ctypes.c_double),
-                ("epochs", ctypes.c_int64)]
+                ("epochs", ctypes.c_int64), ("ray_steps_unfinished", ctypes.c_double)]
 
 
 # name -> (restype, argtypes); every exported symbol of include/geon_gpu.h

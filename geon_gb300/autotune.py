@@ -15,7 +15,11 @@ from . import _ffi
 from ._util import check
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "autotune.json")
-VARIANTS = ("no register cap", "8 blocks/SM (<=64 regs)", "10 blocks/SM (<=51 regs)")
+CAPS = ("no register cap", "<=64 registers", "<=51 registers")
+BLOCKS = (128, 64, 256)
+# source 0 (camera rays, ray arrays): the register caps at 128 threads per block;
+# source 1 (equatorial shadow rays): cap + 3 * block-size index
+VARIANTS = tuple(f"{c}, {b} threads/block" for b in BLOCKS for c in CAPS)
 
 
 def _gpu_name():
@@ -40,18 +44,19 @@ def autotune(metric, n_rays=0, max_steps=20000, use_cache=True):
     Returns {"variant": [camera/array source, equatorial source], "rates": ...}.
     """
     lib = _ffi.load()
-    key = f"{_gpu_name()}|kind={metric.kind}|rays={n_rays}|steps={max_steps}"
+    key = f"{_gpu_name()}|kind={metric.kind}|rays={n_rays}|steps={max_steps}|variants={len(VARIANTS)}"
     cache = _load() if use_cache else {}
     if key in cache:
         for src, v in enumerate(cache[key]["variant"]):
             if v >= 0:
                 check(lib.geon_set_mixed_variant(metric.kind, src, int(v)))
         return cache[key]
-    rates = (ctypes.c_double * 6)()
+    rates = (ctypes.c_double * 12)()
     best = (ctypes.c_int * 2)()
     check(lib.geon_autotune_mixed(metric.handle, int(n_rays), int(max_steps), rates, best))
     entry = {"variant": [int(best[0]), int(best[1])],
              "rates": {"camera": [float(r) for r in rates[:3]], "equatorial": [float(r) for r in rates[3:]]},
+             "block_size": {"camera": 128, "equatorial": BLOCKS[int(best[1]) // 3] if best[1] >= 0 else None},
              "variants": list(VARIANTS), "calibration": {"rays": int(n_rays), "max_steps": int(max_steps)}}
     if use_cache:
         cache[key] = entry

@@ -282,7 +282,7 @@ void geon_set_persistent_reserve_f(double blocks_per_sm) {
 
 int geon_set_mixed_variant(int kind, int source, int variant) {
   if (kind < GEON_MINKOWSKI || kind > GEON_MORRIS_THORNE || source < 0 || source > 1 || variant < 0 ||
-      variant >= MIXED_VARIANTS)
+      variant >= (source == 1 ? MIXED_VARIANTS : MIXED_CAPS))
     return fail(GEON_ERR_INVALID, "bad kind, source or variant");
   g_variant[kind][source].store(variant);
   return GEON_OK;
@@ -299,17 +299,19 @@ int geon_get_mixed_variant(int kind, int source) {
 //    60-degree view from the metric's usual observer, step 0.05;
 //  source 1 (equatorial shadow rays, Schwarzschild only): n launch angles
 //    spread over [10, 20] degrees from r = 20M, step 0.01.
-// Every ray is capped at max_steps. rates_out[2*3] receives ray-steps/s per
-// (source, variant); best_out[2] the chosen variant per source (-1: not tuned).
+// Every ray is capped at max_steps. rates_out[3 + 9] receives ray-steps/s per
+// (source, variant): 3 register caps for source 0, then 9 (cap + 3 x block size
+// 128/64/256) for source 1; best_out[2] the chosen variant per source (-1: not
+// tuned).
 static int time_variants(const TraceLaunch& base, int src, int sink, int64_t n, const int64_t* d_steps,
-                         cudaStream_t s, double* rates, int* best) {
+                         cudaStream_t s, double* rates, int* best, int nvariants) {
   cudaEvent_t a, b;
   GEON_CUDA(cudaEventCreate(&a));
   GEON_CUDA(cudaEventCreate(&b));
   double best_rate = -1.0;
   *best = 0;
   std::vector<int64_t> st(n);
-  for (int v = 0; v < MIXED_VARIANTS; ++v) {
+  for (int v = 0; v < nvariants; ++v) {
     TraceLaunch L = base;
     L.variant = v;
     float best_ms = 1e30f;
@@ -352,7 +354,7 @@ int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, doub
     n_rays = (int64_t)sms * 6 * 128 * 4;  // 128 threads per trace block
   }
   const int kind = m->desc.kind;
-  double rates[6] = {0, 0, 0, 0, 0, 0};
+  double rates[MIXED_CAPS + MIXED_VARIANTS] = {};
   int best[2] = {0, -1};
   cudaStream_t s = host_stream();
   geon_camera cam;
@@ -383,7 +385,8 @@ int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, doub
   L.show_stars = 1;
   L.queue = ws.as<unsigned long long>();
   L.flags = reinterpret_cast<int*>(L.queue + 1);
-  if (int rc = time_variants(L, SRC_CAMERA, SINK_RENDER, n, dsteps.as<int64_t>(), s, rates, &best[0])) return rc;
+  if (int rc = time_variants(L, SRC_CAMERA, SINK_RENDER, n, dsteps.as<int64_t>(), s, rates, &best[0], MIXED_CAPS))
+    return rc;
   g_variant[kind][0].store(best[0]);
   if (kind == GEON_SCHWARZSCHILD) {
     std::vector<double> alpha(n);
@@ -398,7 +401,8 @@ int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, doub
     E.steps = dsteps.as<int64_t>();
     E.queue = ws.as<unsigned long long>();
     E.flags = reinterpret_cast<int*>(E.queue + 1);
-    if (int rc = time_variants(E, SRC_EQUATORIAL, SINK_SHADOW, n, dsteps.as<int64_t>(), s, rates + 3, &best[1]))
+    if (int rc = time_variants(E, SRC_EQUATORIAL, SINK_SHADOW, n, dsteps.as<int64_t>(), s, rates + MIXED_CAPS,
+                               &best[1], MIXED_VARIANTS))
       return rc;
     g_variant[kind][1].store(best[1]);
   }
@@ -914,13 +918,26 @@ int geon_equatorial_rays(geon_metric_t m, double r_obs, const double* alpha, siz
 }
 
 // Classify rays launched at the given angles on stream s (device buffers).
+// Sweeps of at least SHADOW_ORDER_MIN rays (and fewer than 2^31) are claimed
+// longest first (launch_shadow_order); smaller ones in index order.
+constexpr int64_t SHADOW_ORDER_MIN = 65536;
+
 static int classify_dev(geon_metric_t m, double r_obs, const double* d_alpha, int64_t n, double step,
                         int64_t max_steps, int precision, int32_t* d_term, int64_t* d_steps,
                         cudaStream_t s) {
-  DBuf ws;
-  GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 2, s));
-  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 2, s));
+  DBuf ws, dorder;
+  GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 4, s));
+  GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 4, s));
+  const int32_t* order = nullptr;
+  if (n >= SHADOW_ORDER_MIN && n < ((int64_t)1 << 31)) {
+    GEON_CUDA(dorder.alloc(sizeof(int32_t) * n, s));
+    counted();
+    GEON_CUDA(launch_shadow_order(m->desc.p[0], r_obs, d_alpha, n, dorder.as<int32_t>(),
+                                  ws.as<unsigned long long>() + 2, s));
+    order = dorder.as<int32_t>();
+  }
   TraceLaunch L = base_launch(m, step, max_steps);
+  L.order = order;
   L.n = n;
   L.alpha = d_alpha;
   L.r_obs = r_obs;

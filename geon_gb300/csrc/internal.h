@@ -50,7 +50,10 @@ struct CameraDesc {
 };
 
 enum : int { MIXED_REPROJECT = 1, MIXED_ORBIT = 2 };
-constexpr int MIXED_VARIANTS = 3;
+// mixed-kernel variants: register cap (none, 64, 51 registers) x block size
+// (128, 64, 256; block sizes other than 128 only for the equatorial source)
+constexpr int MIXED_CAPS = 3;
+constexpr int MIXED_VARIANTS = 9;
 
 // A regular grid of points for curvature jobs (geon_grid of the ABI).
 struct GridDesc {
@@ -95,6 +98,7 @@ struct TraceLaunch {
   // adaptive stepping (GEON_ADAPTIVE): error tolerances
   double rtol, atol;
   // work queue
+  const int32_t* order;       // the k-th claimed ray is order[k] (null: ray k); n < 2^31 when set
   unsigned long long* queue;  // next unclaimed ray index
   int* flags;                 // bit 0: a metric became singular (inverse of g failed)
 };
@@ -148,6 +152,12 @@ cudaError_t launch_bisect_walk(int64_t nb, int64_t per, int levels, const double
 cudaError_t launch_bisect_finish(int64_t nb, const double* lo, const double* hi, double* alpha_c,
                                  cudaStream_t s);
 cudaError_t launch_fma_probe(int fp64, void* out, int blocks, int threads, int iters, cudaStream_t s);
+// Claim order of a shadow sweep, longest rays first: order[] gets the indices of
+// the rays whose impact parameter is at least 0.998 b_c (escaping or orbiting
+// near the photon sphere: the long paths) from the front and the others from
+// the back; counters (2 x u64, zeroed by the caller) are the two fill levels.
+cudaError_t launch_shadow_order(double m, double r_obs, const double* alpha, int64_t n, int32_t* order,
+                                unsigned long long* counters, cudaStream_t s);
 
 // ---- launchers (curvature_fp64.cu) ----
 // what: 0 riemann, 1 ricci, 2 ricci_scalar, 3 einstein, 4 stress_energy, 5 nec

@@ -198,6 +198,7 @@ struct geon_server {
   std::vector<double> lat[3];
   int64_t submitted = 0, completed = 0, failed = 0;
   double ray_steps = 0, grid_points = 0, t_first = -1, t_last = 0;
+  double ray_steps_unfinished = 0;  // steps of the finished rays of cancelled / timed-out requests
   int64_t epochs = 0;
   uint64_t gen = 0;  // bumped by every submission and completion
   bool in_launch = false;  // a serving launch is on the GPU (the graph may not change)
@@ -382,6 +383,7 @@ void finish(geon_server* S, HostJob* J, int error) {
   J->state = ST_DONE;
   if (error) {
     ++S->failed;
+    S->ray_steps_unfinished += J->ray_steps;
   } else {
     ++S->completed;
     S->lat[J->spec.type].push_back(1e3 * (J->t_done - J->t_submit));
@@ -536,6 +538,7 @@ void server_loop(geon_server* S) {
       if (!J->tracing) continue;
       if (J->stop_flagged) {
         if (S->epochs > J->stop_epoch) {  // a full launch since the flag: no lane holds the slot
+          J->ray_steps += (double)S->h_counters[2 * SERVE_MAX_JOBS + J->slot];  // its finished rays
           J->tracing = false;
           hand_off(S, J);
         }
@@ -753,7 +756,14 @@ int geon_server_create(size_t budget_bytes, geon_server_t* out) {
   cudaMemcpy(S->d_cls, hc.data(), sizeof(ServeClass) * SERVE_CLASSES, cudaMemcpyHostToDevice);
   cudaStreamCreateWithFlags(&S->s_main, cudaStreamNonBlocking);
   cudaStreamCreateWithFlags(&S->s_walk, cudaStreamNonBlocking);
-  cudaStreamCreateWithFlags(&S->s_side, cudaStreamNonBlocking);
+  // Curvature grid kernels run on s_side at the highest stream priority: the
+  // persistent ray kernels hold every SM for one launch (a few ms), and when
+  // they end the block scheduler takes the waiting curvature blocks first, so a
+  // curvature request runs at nearly the full GPU's rate between two launches
+  // instead of trickling into the slots the ray kernels leave.
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  cudaStreamCreateWithPriority(&S->s_side, cudaStreamNonBlocking, prio_greatest);
   cudaStreamCreateWithFlags(&S->s_done, cudaStreamNonBlocking);
   for (int c = 0; c < SERVE_CLASSES; ++c) {
     cudaStreamCreateWithFlags(&S->s_cls[c], cudaStreamNonBlocking);
@@ -967,6 +977,7 @@ int geon_server_stats_get(geon_server_t S, geon_server_stats* out) {
   for (double x : all) sum += x;
   out->mean_ms = all.empty() ? 0.0 : sum / (double)all.size();
   out->ray_steps = S->ray_steps;
+  out->ray_steps_unfinished = S->ray_steps_unfinished;
   out->grid_points = S->grid_points;
   out->wall_s = S->t_first < 0 ? 0.0 : (S->t_last - S->t_first);
   out->epochs = S->epochs;

@@ -116,6 +116,43 @@ constexpr int TRACE_BLOCK = 128;
 constexpr int TRACE_INNER = 16;
 enum : int { STEP_NONFINITE = 0, STEP_OK = 1, STEP_HORIZON = 2 };
 
+// Up to TRACE_INNER steps of one ray (geodesic.rs:71-116): the step cap, the
+// termination test before every step, the step, its NaN guard. n = steps the
+// ray has taken so far; returns the new count. On termination sets t and
+// taken (steps_taken of the reference: max_steps at the cap, the steps before
+// a test that ends the ray or a non-finite step, one more after a horizon
+// step). The counts inside the group are 32-bit; the ray's total is 64-bit.
+template <class Stepper>
+__device__ __forceinline__ int64_t group_steps(Stepper& st, const TraceLaunch& L, int64_t max_steps, int64_t n,
+                                               int& t, int64_t& taken) {
+  const int64_t left64 = max_steps - n;
+  const int left = left64 < (int64_t)TRACE_INNER ? (int)left64 : TRACE_INNER;
+  int done = 0, extra = 0;
+#pragma unroll 1
+  for (int inner = 0; inner < TRACE_INNER; ++inner) {
+    if (done >= left) {  // loop exhausted: Diverged with steps_taken = max_steps
+      t = TERM_DIVERGED;
+      break;
+    }
+    t = st.terminate(L);
+    if (t != TERM_NONE) break;
+    const int r = st.step(L);
+    if (r == STEP_OK) {
+      ++done;
+    } else if (r == STEP_NONFINITE) {
+      t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
+      break;
+    } else {
+      t = TERM_CAPTURED;
+      extra = 1;
+      break;
+    }
+  }
+  n += done;
+  taken = n + extra;
+  return n;
+}
+
 // geodesic.rs:62-117 for every ray of the job, persistent over a work queue.
 // Stepper owns the ray state: load(y0), to_double(y), terminate(L), step(L)
 // returning STEP_OK (advanced), STEP_NONFINITE (state unchanged: Diverged) or
@@ -140,7 +177,7 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
       if (ray < 0) {
         const unsigned long long idx = base + __popc(need & lt_mask);
         if (idx < (unsigned long long)L.n) {
-          ray = (int64_t)idx;
+          ray = L.order ? (int64_t)L.order[idx] : (int64_t)idx;
           n = 0;
           double y0[8];
           load_ray<SRC>(L, ray, y0);
@@ -150,34 +187,14 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
     }
     if (__ballot_sync(FULL, ray >= 0) == 0) break;
     if (ray >= 0) {
-#pragma unroll 1
-      for (int inner = 0; inner < TRACE_INNER; ++inner) {
-        int t = TERM_NONE;
-        int64_t taken = n;
-        if (n >= L.max_steps) {  // loop exhausted: Diverged with steps_taken = max_steps
-          t = TERM_DIVERGED;
-          taken = L.max_steps;
-        } else {
-          t = st.terminate(L);
-          if (t == TERM_NONE) {
-            const int r = st.step(L);
-            if (r == STEP_OK) {
-              ++n;
-            } else if (r == STEP_NONFINITE) {
-              t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
-            } else {
-              t = TERM_CAPTURED;
-              taken = n + 1;
-            }
-          }
-        }
-        if (t != TERM_NONE) {
-          double y[8];
-          st.to_double(y);
-          store_ray<K, SINK>(L, ray, t, y, taken);
-          ray = -1;
-          break;
-        }
+      int t = TERM_NONE;
+      int64_t taken = 0;
+      n = group_steps(st, L, L.max_steps, n, t, taken);
+      if (t != TERM_NONE) {
+        double y[8];
+        st.to_double(y);
+        store_ray<K, SINK>(L, ray, t, y, taken);
+        ray = -1;
       }
     }
   }
@@ -244,35 +261,14 @@ __device__ __forceinline__ void trace_loop_multi(const TraceLaunch* __restrict__
     if (__ballot_sync(FULL, job >= 0) == 0) break;
     if (job >= 0) {
       const TraceLaunch& L = jobs[job];
-      const int64_t max_steps = L.max_steps;
-#pragma unroll 1
-      for (int inner = 0; inner < TRACE_INNER; ++inner) {
-        int t = TERM_NONE;
-        int64_t taken = n;
-        if (n >= max_steps) {
-          t = TERM_DIVERGED;
-          taken = max_steps;
-        } else {
-          t = st.terminate(L);
-          if (t == TERM_NONE) {
-            const int r = st.step(L);
-            if (r == STEP_OK) {
-              ++n;
-            } else if (r == STEP_NONFINITE) {
-              t = TERM_DIVERGED;
-            } else {
-              t = TERM_CAPTURED;
-              taken = n + 1;
-            }
-          }
-        }
-        if (t != TERM_NONE) {
-          double y[8];
-          st.to_double(y);
-          store_ray_any<SINK>(L, L.M.kind, ray, t, y, taken);
-          job = -1;
-          break;
-        }
+      int t = TERM_NONE;
+      int64_t taken = 0;
+      n = group_steps(st, L, L.max_steps, n, t, taken);
+      if (t != TERM_NONE) {
+        double y[8];
+        st.to_double(y);
+        store_ray_any<SINK>(L, L.M.kind, ray, t, y, taken);
+        job = -1;
       }
     }
   }

@@ -519,6 +519,46 @@ cudaError_t launch_equatorial_rays(double m, double r_obs, const double* alpha, 
   return cudaGetLastError();
 }
 
+// Longest-first claim order of a shadow sweep (see internal.h). A ray's path
+// length is set by its impact parameter b = r_obs sin(alpha) / sqrt(1 - 2M/r_obs)
+// (bin/validate_shadow.rs:78-79): b > b_c = 3 sqrt(3) M escapes and runs to the
+// escape radius, b near b_c orbits the photon sphere first, b < b_c falls in
+// after a short path. Claiming the long ones first leaves short rays for the
+// end of the sweep, when lanes run out of work. Only the order changes: each
+// ray is integrated the same way wherever it runs.
+__global__ void shadow_order_kernel(double m, double r_obs, const double* __restrict__ alpha, int64_t n,
+                                    int32_t* __restrict__ order, unsigned long long* counters) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  bool is_long = false;
+  if (valid) {
+    const double b = r_obs * sin(alpha[i]) / sqrt(1.0 - 2.0 * m / r_obs);
+    is_long = !(b < 0.998 * 5.196152422706632 * m);  // 3 sqrt(3) M; NaN angles go first
+  }
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const unsigned want_long = __ballot_sync(FULL, valid && is_long);
+  const unsigned want_short = __ballot_sync(FULL, valid && !is_long);
+  unsigned long long bl = 0, bs = 0;
+  if (lane == 0) {
+    if (want_long) bl = atomicAdd(&counters[0], (unsigned long long)__popc(want_long));
+    if (want_short) bs = atomicAdd(&counters[1], (unsigned long long)__popc(want_short));
+  }
+  bl = __shfl_sync(FULL, bl, 0);
+  bs = __shfl_sync(FULL, bs, 0);
+  if (!valid) return;
+  if (is_long) order[bl + __popc(want_long & lt)] = (int32_t)i;
+  else order[n - 1 - (int64_t)(bs + __popc(want_short & lt))] = (int32_t)i;
+}
+
+cudaError_t launch_shadow_order(double m, double r_obs, const double* alpha, int64_t n, int32_t* order,
+                                unsigned long long* counters, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  shadow_order_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m, r_obs, alpha, n, order, counters);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Device-side bisection rounds (bin/validate_shadow.rs:70-79, L levels per round)
 // ---------------------------------------------------------------------------

@@ -501,33 +501,36 @@ struct MixedStepperAny : MixedCore<FEAT> {
   }
 };
 
-// MINB is the register cap chosen by the autotuner: __launch_bounds__(128, MINB)
-// asks the compiler to fit MINB blocks per SM (1: no cap, 63 registers and 8
-// blocks for the planar equatorial step, 72 and 7 for the camera step; 8: <= 64
-// registers; 10: <= 51), trading registers (and spills) for resident warps.
-template <int K, int SRC, int SINK, int MINB, int FEAT>
-__global__ void __launch_bounds__(TRACE_BLOCK, MINB) trace_mixed_kernel(const TraceLaunch L) {
+// MINB is the register cap chosen by the autotuner: __launch_bounds__(BLOCK,
+// MINB) asks the compiler to fit MINB blocks per SM (1: no cap, 63 registers
+// and 8 blocks of 128 for the planar equatorial step, 72 and 7 for the camera
+// step; 8 blocks of 128: <= 64 registers; 10: <= 51), trading registers (and
+// spills) for resident warps. BLOCK is the block size (128 except for the
+// equatorial shadow kernel, whose autotuner also tries 64 and 256).
+template <int K, int SRC, int SINK, int MINB, int FEAT, int BLOCK = TRACE_BLOCK>
+__global__ void __launch_bounds__(BLOCK, MINB) trace_mixed_kernel(const TraceLaunch L) {
   constexpr int PL = (SRC == SRC_EQUATORIAL && K == KIND_SCHWARZSCHILD) ? FEAT_PLANAR : 0;
   trace_loop<MixedStepper<K, FEAT | PL>, K, SRC, SINK>(L);
 }
 
-template <int K, int SRC, int SINK, int MINB, int FEAT>
+template <int K, int SRC, int SINK, int MINB, int FEAT, int BLOCK = TRACE_BLOCK>
 static cudaError_t launch_mst_v(const TraceLaunch& L, cudaStream_t s) {
   static int sms = 0, per_sm = 0;
   if (sms == 0) {
     int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_mixed_kernel<K, SRC, SINK, MINB, FEAT>, TRACE_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_mixed_kernel<K, SRC, SINK, MINB, FEAT, BLOCK>, BLOCK,
+                                                  0);
     per_sm = occ < 1 ? 1 : occ;
   }
-  // persistent grid: every resident slot, minus the blocks per SM the caller
-  // keeps free for a concurrent job
-  const int64_t slots = persistent_slots(sms, per_sm, L.reserve_per_sm);
-  const int64_t need = (L.n + TRACE_BLOCK - 1) / TRACE_BLOCK;
+  // persistent grid: every resident slot, minus what the caller keeps free for
+  // a concurrent job (counted in slots of TRACE_BLOCK threads)
+  const int64_t slots = persistent_slots(sms, per_sm, L.reserve_per_sm * (float)TRACE_BLOCK / (float)BLOCK);
+  const int64_t need = (L.n + BLOCK - 1) / BLOCK;
   int grid = (int)(need < slots ? need : slots);
   if (grid < 1) grid = 1;
-  trace_mixed_kernel<K, SRC, SINK, MINB, FEAT><<<grid, TRACE_BLOCK, 0, s>>>(L);
+  trace_mixed_kernel<K, SRC, SINK, MINB, FEAT, BLOCK><<<grid, BLOCK, 0, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -539,7 +542,7 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
     // orbit-plane frame (the default for camera rays and ray arrays of the
     // spherically symmetric metrics; equatorial rays already step on their plane)
     if (feat == 0 && (L.mixed_flags & MIXED_ORBIT)) {
-      switch (L.variant) {
+      switch (L.variant % 3) {
         case 1: return launch_mst_v<K, SRC, SINK, 8, FEAT_ORBIT>(L, s);
         case 2: return launch_mst_v<K, SRC, SINK, 10, FEAT_ORBIT>(L, s);
         default: return launch_mst_v<K, SRC, SINK, 1, FEAT_ORBIT>(L, s);
@@ -551,10 +554,26 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
     case FEAT_REPROJECT: return launch_mst_v<K, SRC, SINK, 1, FEAT_REPROJECT>(L, s);
     case FEAT_BAND | FEAT_REPROJECT: return launch_mst_v<K, SRC, SINK, 1, FEAT_BAND | FEAT_REPROJECT>(L, s);
   }
-  switch (L.variant) {
-    case 1: return launch_mst_v<K, SRC, SINK, 8, 0>(L, s);
-    case 2: return launch_mst_v<K, SRC, SINK, 10, 0>(L, s);
-    default: return launch_mst_v<K, SRC, SINK, 1, 0>(L, s);
+  if constexpr (SRC == SRC_EQUATORIAL && SINK == SINK_SHADOW) {
+    // variant = register cap + 3 * block size (128, 64, 256); the same caps in
+    // registers per thread (64, 51) at every block size
+    switch (L.variant) {
+      case 1: return launch_mst_v<K, SRC, SINK, 8, 0>(L, s);
+      case 2: return launch_mst_v<K, SRC, SINK, 10, 0>(L, s);
+      case 3: return launch_mst_v<K, SRC, SINK, 1, 0, 64>(L, s);
+      case 4: return launch_mst_v<K, SRC, SINK, 16, 0, 64>(L, s);
+      case 5: return launch_mst_v<K, SRC, SINK, 20, 0, 64>(L, s);
+      case 6: return launch_mst_v<K, SRC, SINK, 1, 0, 256>(L, s);
+      case 7: return launch_mst_v<K, SRC, SINK, 4, 0, 256>(L, s);
+      case 8: return launch_mst_v<K, SRC, SINK, 5, 0, 256>(L, s);
+      default: return launch_mst_v<K, SRC, SINK, 1, 0>(L, s);
+    }
+  } else {
+    switch (L.variant % 3) {
+      case 1: return launch_mst_v<K, SRC, SINK, 8, 0>(L, s);
+      case 2: return launch_mst_v<K, SRC, SINK, 10, 0>(L, s);
+      default: return launch_mst_v<K, SRC, SINK, 1, 0>(L, s);
+    }
   }
 }
 

@@ -197,5 +197,5 @@ class Server:
             "by_type": {names[t]: {"completed": s.completed_by_type[t], "p50_ms": s.p50_ms_by_type[t],
                                    "p99_ms": s.p99_ms_by_type[t]} for t in range(3)},
             "ray_steps": s.ray_steps, "grid_points": s.grid_points, "wall_s": s.wall_s,
-            "launches": s.epochs,
+            "launches": s.epochs, "ray_steps_unfinished": s.ray_steps_unfinished,
         }

@@ -263,14 +263,18 @@ void geon_set_persistent_reserve(int blocks_per_sm);
  * blocks_per_sm)) blocks, so e.g. 4.5 leaves 4 slots on half of the SMs and 5
  * on the others. No counterpart in the reference (no persistent kernels). */
 void geon_set_persistent_reserve_f(double blocks_per_sm);
-/* Register-cap variant of the mixed kernel per metric kind and ray source
- * (source 0: camera rays and ray arrays, 1: equatorial shadow rays): 0 = no
- * cap, 1 = fit 8 blocks of 128 threads per SM, 2 = fit 10. geon_autotune_mixed
- * times every variant on calibration jobs of this metric (n_rays rays - 0 picks
- * four per lane of the widest grid - at most max_steps each; the equatorial job only for Schwarzschild), selects the
- * fastest per source and writes ray-steps/s per (source, variant) to
- * rates_out[6] and the choices to best_out[2] (-1 = source not tuned); either
- * may be NULL. */
+/* Launch variant of the mixed kernel per metric kind and ray source (source 0:
+ * camera rays and ray arrays, 1: equatorial shadow rays). Register cap c: 0 =
+ * none, 1 = at most 64 registers per thread, 2 = at most 51. Source 0 takes
+ * variant = c (blocks of 128 threads); source 1 takes variant = c + 3 b with
+ * block size b: 0 = 128, 1 = 64, 2 = 256 threads. geon_autotune_mixed times
+ * every variant on calibration jobs of this metric (n_rays rays - 0 picks four
+ * per lane of the widest grid - at most max_steps each; the equatorial job only
+ * for Schwarzschild), selects the fastest per source and writes ray-steps/s to
+ * rates_out[12] (3 for source 0, then 9 for source 1) and the choices to
+ * best_out[2] (-1 = source not tuned); either may be NULL. The persistent
+ * reserve (geon_set_persistent_reserve) counts slots of 128 threads whatever
+ * the block size. */
 int geon_set_mixed_variant(int kind, int source, int variant);
 int geon_get_mixed_variant(int kind, int source);
 int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, double* rates_out,
@@ -426,6 +430,8 @@ typedef struct {
   double grid_points;                       /* curvature points of completed requests */
   double wall_s;                            /* first submission to last completion */
   int64_t epochs;                           /* persistent-kernel launches */
+  double ray_steps_unfinished;              /* ray-steps of the rays that finished in requests
+                                               that were cancelled or timed out */
 } geon_server_stats;
 
 /* budget_bytes: device memory for request buffers (a request larger than it is
