@@ -57,13 +57,13 @@ N_SWEEP = 1 << 20
 N_BRACKETS = 64
 ITERS = 40
 SCHW = [1.0, 1.001, 1000.0]
-# Block slots per SM the persistent sweep grid leaves to the concurrent bisection
-# rounds. The bisection is a chain of dependent rounds (latency-bound), the sweep
-# throughput-bound: with 8 resident blocks per SM (the planar equatorial step,
-# 63-64 registers) and 16 steps per refill, leaving 5 balances the two (measured on
-# GB300 at 16384 rays per round: 4 -> 1.39e11, 5 -> 1.43e11 ray-steps/s; sweep /
-# bisection 463 / 362 ms at 5, 439 / 475 ms at 4; fractional 4.25-4.75 slower).
-RESERVE = 5
+# Slots of 128 threads per SM the persistent sweep grid leaves to the concurrent
+# bisection rounds. The bisection is a chain of dependent rounds (latency-bound),
+# the sweep throughput-bound: with 8 resident slots per SM (the planar
+# equatorial step, 64 registers) and the longest-first sweep order, leaving 4
+# balances the two (measured on GB300: sweep / bisection 388 / 392 ms at 4, 415 /
+# 295 ms at 5, 484 / 219 ms at 6; 1.68e11, 1.59e11, 1.36e11 ray-steps/s).
+RESERVE = 4
 BISECT_RAYS = 16384  # speculative width of a bisection round (geon_set_bisect_rays_per_round)
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
 CURV_FLOPS_PER_POINT = 20000  # Alcubierre: 9 FD Christoffel evaluations, Riemann, contractions, 16 T(k, k)
@@ -277,7 +277,10 @@ def main():
     ap.add_argument("--reserve", type=float, default=RESERVE,
                     help="block slots per SM the sweep leaves free for the bisections (latency vs throughput)")
     ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy and FP64 legs trace every k-th sweep ray")
-    ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 latency leg")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the FP64 latency leg")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="mixed equatorial kernel variant (register cap + 3 x block size index); -1: the autotuner's")
+    ap.add_argument("--sweep-order", type=int, default=1, help="longest-first claim order of the sweep (1) or not (0)")
     ap.add_argument("--legs", default="all",
                     help="comma list of legs beside the headline (accuracy,fp64,e2e,cpu,config1,config3,config4,"
                          "r30), 'all' or 'none'")
@@ -317,6 +320,9 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     run = SweepRunner(lib, torch, m.handle, args, dev)
     lib.geon_set_bisect_rays_per_round(args.bisect_rays)
+    lib.geon_set_sweep_order(args.sweep_order)
+    if args.variant >= 0:
+        lib.geon_set_mixed_variant(1, 1, args.variant)
     bis = not args.sweep_only
 
     def barrier():
@@ -385,7 +391,7 @@ def main():
     if "config1" in legs:
         extras["config1"] = leg("config1", config1_leg, geon, lib, peak64)
     if "config3" in legs:
-        extras["config3"] = leg("config3", config3_leg, geon, lib, 2048, 64)
+        extras["config3"] = leg("config3", config3_leg, geon, lib, 2048, 128, 0)
     if "config4" in legs:
         extras["config4"] = leg("config4", config4_leg, geon, 128, peak64)
     if "r30" in legs:
@@ -405,8 +411,9 @@ def main():
                    "precision": args.precision, "rays_per_gpu": N_SWEEP, "bisections_per_gpu": N_BRACKETS,
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards",
                    "sweep_reserve_blocks_per_sm": args.reserve, "bisect_rays_per_round": args.bisect_rays,
-                   "mixed_kernel_variant": None if tuned is None else tuned["variant"][1],
-                   "mixed_block_size": None if tuned is None else tuned.get("block_size", {}).get("equatorial"),
+                   "mixed_kernel_variant": lib.geon_get_mixed_variant(1, 1) if prec == 1 else None,
+                   "mixed_block_size": (128, 64, 256)[lib.geon_get_mixed_variant(1, 1) // 3] if prec == 1 else None,
+                   "sweep_claim_order": "longest first" if args.sweep_order else "index order",
                    "autotune_rates": None if tuned is None else tuned.get("rates")},
         "latency": {"step_ms_p50": pct(times, 50), "step_ms_p99": pct(times, 99),
                     "bisection_ms_p50": pct([r["bisection_ms"] for r in res], 50),
@@ -632,7 +639,7 @@ def config1_leg(geon, lib, peak64):
     return out
 
 
-def config3_leg(geon, lib, n, row_step):
+def config3_leg(geon, lib, n, row_step, check_agreeing=256):
     """BASELINE config 3: 2048^2 Alcubierre (R 2, thickness 0.125, v 0.5,
     observer x = -10 looking +x) and Morris-Thorne (b0 1, observer l = 10)
     renders, fov 90, h 0.05, cap 20000: mixed on the full images; FP64 (the
@@ -657,11 +664,15 @@ def config3_leg(geon, lib, n, row_step):
         r64 = geon.trace(m, y0, 0.05, 20000, precision="fp64")
         dt64 = time.perf_counter() - t0
         rmx = geon.trace(m, y0, 0.05, 20000, precision="mixed")
-        rep = geon.accuracy.class_report(m, y0, 0.05, 20000, rmx.termination, r64.termination)
+        # the check of agreeing rays re-traces rays that run to the 20000-step cap
+        # at 16 sub-steps per step, one warp's latency through the finite-difference
+        # Christoffel symbols (~25 s): the tests run it, the default bench line not
+        rep = geon.accuracy.class_report(m, y0, 0.05, 20000, rmx.termination, r64.termination,
+                                         check_agreeing=check_agreeing)
         esc = geon.accuracy.clean_escapes(m, r64) & geon.accuracy.clean_escapes(m, rmx)
         d64 = m.asymptotic_direction(r64.final_state[esc])
         dmx = m.asymptotic_direction(rmx.final_state[esc])
-        ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0)) if esc.any() else np.zeros(1)
+        ang = np.arccos(np.clip(np.sum(d64 * dmx, axis=1), -1.0, 1.0)) if esc.any() else None
         yc = y0[:n]  # the first sampled row
         t0 = time.perf_counter()
         _, _, osteps, _ = orc.trace(kind, params, yc, 0.05, 20000, math=orc.LIBM, nthreads=threads)
@@ -672,8 +683,10 @@ def config3_leg(geon, lib, n, row_step):
                      "fp64_sample": f"every {row_step}th row ({len(y0)} rays), host API wall time",
                      "mixed_over_fp64": (st.total_steps / dt) / (float(r64.steps_taken.sum()) / dt64),
                      "classes_vs_fp64": rep,
-                     "escape_dir_err_rad_p50": float(np.median(ang)), "escape_dir_err_rad_p99":
-                         float(np.quantile(ang, 0.99)), "escape_dir_err_rad_max": float(ang.max()),
+                     "escapes_compared": int(esc.sum()),
+                     "escape_dir_err_rad_p50": None if ang is None else float(np.median(ang)),
+                     "escape_dir_err_rad_p99": None if ang is None else float(np.quantile(ang, 0.99)),
+                     "escape_dir_err_rad_max": None if ang is None else float(ang.max()),
                      "cpu_baseline": {"value": float(osteps.sum()) / dt_cpu, "unit": "ray-steps/s", "cores": threads,
                                       "kind": "port", "sample": f"row 0 ({len(yc)} rays, {dt_cpu:.1f} s)"}}
     out["mixed_ray_steps_per_s_both"] = (sum(out[c]["mixed_total_steps"] for c in cases)

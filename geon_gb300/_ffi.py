@@ -127,6 +127,10 @@ SIGNATURES = {
     "geon_set_mixed_reproject": (None, [ctypes.c_int]),
     "geon_set_mixed_orbit_plane": (None, [ctypes.c_int]),
     "geon_get_mixed_orbit_plane": (ctypes.c_int, []),
+    "geon_set_mixed_null_fix": (None, [ctypes.c_int]),
+    "geon_set_sweep_order": (None, [ctypes.c_int]),
+    "geon_get_sweep_order": (ctypes.c_int, []),
+    "geon_get_mixed_null_fix": (ctypes.c_int, []),
     "geon_set_persistent_reserve": (None, [ctypes.c_int]),
     "geon_set_persistent_reserve_f": (None, [ctypes.c_double]),
     "geon_set_mixed_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),

@@ -8,7 +8,9 @@ Christoffel symbols where they blow up, and the ray is flung to r ~ 1e30 or
 overflows (the reference then reports it Escaped or Diverged,
 schwarzschild.rs:109-121, geodesic.rs:89-100). Where another trace (the mixed
 path, the fast FP64 mode) assigns a ray a different class, the ray is traced
-again in FP64 with 16 RK4 sub-steps per step. Termination is tested at every
+again in FP64 with 16 RK4 sub-steps per step (Schwarzschild rays with the
+planar step of GEON_FP64_FAST, the others with the FP64 parity stepper).
+Termination is tested at every
 sub-step, so a ray that reaches the capture radius between two of the
 reference's tests is captured there; the step cap is the reference's (a ray
 escapes only if it does so by the reference's last test, at step
@@ -75,7 +77,11 @@ def arbiter_classes(metric, y0, step, max_steps):
     if metric.kind in (SCHWARZSCHILD, MORRIS_THORNE):
         y0 = orbit_frame_states(y0)
     cap = SUBSTEPS * (int(max_steps) - 1) + 1 if max_steps > 0 else 0
-    return trace(metric, y0, step / SUBSTEPS, cap, precision="fp64").termination
+    # Schwarzschild rays on their plane take the planar FP64 step of
+    # GEON_FP64_FAST (same RK4 and tests, fused arithmetic, no trigonometry);
+    # the other metrics the FP64 parity stepper
+    prec = "fp64fast" if metric.kind == SCHWARZSCHILD else "fp64"
+    return trace(metric, y0, step / SUBSTEPS, cap, precision=prec).termination
 
 
 def class_report(metric, y0, step, max_steps, term, term_fp64, check_agreeing=256, seed=0):
@@ -103,5 +109,6 @@ def class_report(metric, y0, step, max_steps, term, term_fp64, check_agreeing=25
         "agreeing_rays_checked": int(len(chk)),
         "agreeing_rays_arbiter_differs": int(np.sum(arb_chk != term[chk])),
         "arbiter": f"FP64 RK4 at step/{SUBSTEPS}, termination tested every sub-step, the reference's cap"
+                   + (" (planar fast-FP64 step)" if metric.kind == SCHWARZSCHILD else "")
                    + (", orbit-plane frame" if metric.kind in (SCHWARZSCHILD, MORRIS_THORNE) else ""),
     }

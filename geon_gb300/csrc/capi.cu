@@ -30,6 +30,8 @@ std::atomic<int> g_show_stars{1};
 std::atomic<float> g_band[4] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
 std::atomic<int> g_reproject{0};
 std::atomic<int> g_orbit{1};  // orbit-plane frame of the mixed path (default on)
+std::atomic<int> g_nullfix{1};  // compensated null re-projection every 16 steps (planar steps; default on)
+std::atomic<int> g_sweep_order{1};  // longest-first claim order of shadow sweeps
 std::atomic<float> g_reserve{0.0f};
 std::atomic<double> g_rtol{1e-10};  // GEON_ADAPTIVE error tolerances
 std::atomic<double> g_atol{1e-12};
@@ -141,7 +143,8 @@ TraceLaunch base_launch(geon_metric_t m, double step, int64_t max_steps) {
   L.sixth = step / 6.0;
   L.max_steps = max_steps;
   L.band = g_band[m->desc.kind].load();
-  L.mixed_flags = (g_reproject.load() ? MIXED_REPROJECT : 0) | (g_orbit.load() ? MIXED_ORBIT : 0);
+  L.mixed_flags = (g_reproject.load() ? MIXED_REPROJECT : 0) | (g_orbit.load() ? MIXED_ORBIT : 0) |
+                  (g_nullfix.load() ? MIXED_NULLFIX : 0);
   L.reserve_per_sm = g_reserve.load();
   L.variant = g_variant[m->desc.kind][0].load();
   L.rtol = g_rtol.load();
@@ -251,6 +254,10 @@ double geon_get_mixed_band(int kind) {
 
 void geon_set_mixed_reproject(int on) { g_reproject.store(on ? 1 : 0); }
 void geon_set_mixed_orbit_plane(int on) { g_orbit.store(on ? 1 : 0); }
+void geon_set_mixed_null_fix(int on) { g_nullfix.store(on ? 1 : 0); }
+void geon_set_sweep_order(int on) { g_sweep_order.store(on ? 1 : 0); }
+int geon_get_sweep_order(void) { return g_sweep_order.load(); }
+int geon_get_mixed_null_fix(void) { return g_nullfix.load(); }
 int geon_get_mixed_orbit_plane(void) { return g_orbit.load(); }
 
 int geon_set_bisect_rays_per_round(int64_t rays) {
@@ -929,7 +936,7 @@ static int classify_dev(geon_metric_t m, double r_obs, const double* d_alpha, in
   GEON_CUDA(ws.alloc(sizeof(unsigned long long) * 4, s));
   GEON_CUDA(cudaMemsetAsync(ws.p, 0, sizeof(unsigned long long) * 4, s));
   const int32_t* order = nullptr;
-  if (n >= SHADOW_ORDER_MIN && n < ((int64_t)1 << 31)) {
+  if (g_sweep_order.load() && n >= SHADOW_ORDER_MIN && n < ((int64_t)1 << 31)) {
     GEON_CUDA(dorder.alloc(sizeof(int32_t) * n, s));
     counted();
     GEON_CUDA(launch_shadow_order(m->desc.p[0], r_obs, d_alpha, n, dorder.as<int32_t>(),

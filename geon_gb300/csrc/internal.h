@@ -49,7 +49,7 @@ struct CameraDesc {
   int forward_sign;
 };
 
-enum : int { MIXED_REPROJECT = 1, MIXED_ORBIT = 2 };
+enum : int { MIXED_REPROJECT = 1, MIXED_ORBIT = 2, MIXED_NULLFIX = 4 };
 // mixed-kernel variants: register cap (none, 64, 51 registers) x block size
 // (128, 64, 256; block sizes other than 128 only for the equatorial source)
 constexpr int MIXED_CAPS = 3;

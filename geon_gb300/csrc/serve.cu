@@ -158,6 +158,10 @@ struct HostJob {
 
 int class_of(int kind, int precision) { return kind * 2 + (precision == GEON_MIXED ? 1 : 0); }
 
+// Served mixed requests run the default mixed step whatever the process-wide
+// options say: orbit-plane frame for camera rays, compensated null re-projection.
+constexpr int SERVE_MIXED_FLAGS = MIXED_ORBIT | MIXED_NULLFIX;
+
 }  // namespace
 
 struct geon_server {
@@ -295,6 +299,7 @@ cudaError_t bisect_publish_round(geon_server* S, HostJob* J) {
   ServeJob sj;
   std::memset(&sj, 0, sizeof sj);
   sj.L = trace_launch_defaults(J->metric, J->spec.step, J->spec.max_steps);
+  sj.L.mixed_flags = SERVE_MIXED_FLAGS;
   sj.L.n = J->nrays;
   sj.L.alpha = b.alpha;
   sj.L.r_obs = J->spec.r_obs;
@@ -337,6 +342,7 @@ int start_job(geon_server* S, HostJob* J) {
     ServeJob sj;
     std::memset(&sj, 0, sizeof sj);
     sj.L = trace_launch_defaults(J->metric, q.render.step, q.render.max_steps);
+    sj.L.mixed_flags = SERVE_MIXED_FLAGS;
     sj.L.cam = c;
     sj.L.n = J->nsamp;
     sj.L.srgb = b.srgb;

@@ -92,12 +92,19 @@ __device__ __forceinline__ void rhs_planar(double m, double two_m, double r, dou
 
 }  // namespace fast
 
+// PLANAR: every ray is equatorial (the shadow source). Otherwise a ray that
+// starts on the equator with p^theta = 0 exactly (theta = pi/2 to the double,
+// as equatorial rays and states turned into their orbit-plane frame are)
+// takes the planar step too: the plane is invariant, and the general step
+// would only add the ~1e-16 drift that cos(pi/2 rounded) gives theta.
 template <bool PLANAR>
 struct FastSchwStepper {
   double y[8];
+  bool on_plane = PLANAR;
   __device__ __forceinline__ void load(const TraceLaunch&, const double y0[8]) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) y[i] = y0[i];
+    if (!PLANAR) on_plane = y[2] == 1.5707963267948966 && y[6] == 0.0;
   }
   __device__ __forceinline__ void to_double(double out[8]) const {
 #pragma unroll
@@ -110,7 +117,7 @@ struct FastSchwStepper {
   __device__ __forceinline__ int step(const TraceLaunch& L) {
     const double m = L.M.p[0], two_m = 2.0 * m;
     const double h = L.step, hh = L.half_step;
-    if (PLANAR) {
+    if (PLANAR || on_plane) {
       double k4, k5, k7;
       double p0 = y[4], p1 = y[5], p3 = y[7];
       fast::rhs_planar(m, two_m, y[1], p0, p1, p3, &k4, &k5, &k7);

@@ -50,6 +50,32 @@ __device__ __forceinline__ void renormalise(float& hi, float& lo) {
   hi = s;
 }
 
+// Float-float (hi, lo) products and sums for the compensated null
+// re-projection: the exact rounding error of a product from one fused
+// multiply-add, of a sum from TwoSum; the results are not renormalised (their
+// low words stay far below the high words' ulp for the few operations chained).
+struct FF {
+  float h, l;
+};
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = a.h * b.h;
+  const float e = __fmaf_rn(a.h, b.h, -p);
+  return {p, __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  const float e = (a.h - (s - bb)) + (b.h - bb);
+  return {s, e + (a.l + b.l)};
+}
+// 1 / (hi + lo): the correctly rounded reciprocal of hi and one Newton
+// correction carried in the low word.
+__device__ __forceinline__ FF ff_rcp(FF a) {
+  const float q = __frcp_rn(a.h);
+  const float e = __fmaf_rn(-q, a.h, 1.0f) - q * a.l;  // 1 - q (hi + lo), its leading part exact
+  return {q, q * e};
+}
+
 // (hi + lo) > t for a threshold held as a (hi, lo) pair.
 __device__ __forceinline__ bool ff_gt(float hi, float lo, float thi, float tlo) {
   return (hi - thi) + (lo - tlo) > 0.0f;
@@ -207,6 +233,37 @@ struct MixedCore {
     }
   }
 
+  // Null re-projection of p^t for a ray on its plane (Schwarzschild: equatorial
+  // rays and rays in their orbit-plane frame; Morris-Thorne in its frame): the
+  // residual R = g(p, p) is formed in float-float from the compensated state
+  // (its terms are O(1) and cancel to ~1e-8, below FP32's own precision), and
+  // one Newton step on g(p, p) = 0 in p^t, delta = R / (2 (-g_tt) p^t), is
+  // added to (hi, lo) of p^t by TwoSum. Schwarzschild, theta = pi/2:
+  //   f R = -(f p^t)^2 + (p^r)^2 + f (r p^phi)^2,  f = 1 - 2M/r;
+  // Morris-Thorne: R = -(p^t)^2 + (p^l)^2 + (b0^2 + l^2) (p^phi)^2.
+  template <int K>
+  __device__ __forceinline__ void null_fix_planar() {
+    const FF r = {hi[1], lo[1]}, pt = {hi[4], lo[4]}, pr = {hi[5], lo[5]}, pp = {hi[7], lo[7]};
+    if (K == KIND_SCHWARZSCHILD) {
+      const FF ir = ff_rcp(r);
+      const FF u = ff_mul({C.two_m, 0.0f}, ir);  // 2M / r
+      const FF f = ff_add({1.0f, 0.0f}, {-u.h, -u.l});
+      const FF E = ff_mul(f, pt);
+      const FF w = ff_mul(r, pp);
+      const FF fw2 = ff_mul(f, ff_mul(w, w));
+      const FF E2 = ff_mul(E, E);
+      const FF fR = ff_add(ff_add(ff_mul(pr, pr), fw2), {-E2.h, -E2.l});
+      const float d = (fR.h + fR.l) / (2.0f * f.h * E.h);
+      if (isfinite(d)) two_sum_update(hi[4], lo[4], d);
+    } else if (K == KIND_MORRIS_THORNE) {
+      const FF r2 = ff_add({C.b0sq, 0.0f}, ff_mul(r, r));
+      const FF pt2 = ff_mul(pt, pt);
+      const FF R = ff_add(ff_add(ff_mul(pr, pr), ff_mul(r2, ff_mul(pp, pp))), {-pt2.h, -pt2.l});
+      const float d = (R.h + R.l) / (2.0f * pt.h);
+      if (isfinite(d)) two_sum_update(hi[4], lo[4], d);
+    }
+  }
+
   // A Schwarzschild ray moving inward inside the photon sphere (r < 3M, p^r < 0)
   // has no turning point left: it falls through the horizon. Near the horizon
   // p^t = E/f grows without bound and the fixed step stops resolving it; a step
@@ -351,6 +408,9 @@ struct MixedCore {
       renormalise(hi[4], lo[4]);
       renormalise(hi[5], lo[5]);
       renormalise(hi[7], lo[7]);
+      // every 16 steps of the ray: the same step of every lane of a warp (rays
+      // start at a refill, refills come every 16 steps), so warp-uniform
+      if ((nsteps & 15) == 0 && (L.mixed_flags & MIXED_NULLFIX)) null_fix_planar<K>();
     }
     if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT)) {
       const float x[4] = {hi[0], hi[1], hi[2], hi[3]};
@@ -581,7 +641,7 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
 // the default mixed step per ray, camera rays of the spherically symmetric
 // metrics in their orbit plane when the orbit-plane option is on (as in the
 // single-render kernels, so each image equals its single render).
-__global__ void __launch_bounds__(TRACE_BLOCK) trace_multi_mixed_kernel(const TraceLaunch* jobs, const MultiDesc D) {
+__global__ void __launch_bounds__(TRACE_BLOCK, 5) trace_multi_mixed_kernel(const TraceLaunch* jobs, const MultiDesc D) {
   trace_loop_multi<MixedStepperAny<FEAT_ORBIT_DYN>, SRC_CAMERA, SINK_RENDER>(jobs, D);
 }
 

@@ -242,6 +242,15 @@ void geon_set_mixed_reproject(int on);
  * in the chart whatever this says). No counterpart in the reference. */
 void geon_set_mixed_orbit_plane(int on);
 int geon_get_mixed_orbit_plane(void);
+/* Compensated null re-projection for GEON_MIXED rays on their plane (shadow
+ * rays; Schwarzschild and Morris-Thorne rays in their orbit-plane frame): every
+ * 16 steps of a ray, g(p, p) is formed in float-float from the compensated
+ * state and one Newton step on g(p, p) = 0 in p^t is added to p^t with its
+ * rounding error kept (null drift ~1e-13, the FP64 path's, at ~3 % of the
+ * step's cost). Default on (1); served requests always use it. No counterpart
+ * in the reference. */
+void geon_set_mixed_null_fix(int on);
+int geon_get_mixed_null_fix(void);
 /* Error tolerances of GEON_ADAPTIVE: a step is accepted when
  * sqrt(mean_i((e_i / (atol + rtol * max(|y_i|, |y_new_i|)))^2)) <= 1.
  * Defaults rtol 1e-10, atol 1e-12. Calls made after this use them. */
@@ -341,6 +350,13 @@ int geon_shadow_bisect(geon_metric_t schwarzschild, double r_obs, const double* 
                        size_t nb, int iters, double step, int64_t max_steps, int precision,
                        double* alpha_c, double* lo_out, double* hi_out, int64_t* steps_out);
 
+/* Claim order of geon_shadow_classify(_dev) over 65536 rays or more: 1 (the
+ * default) claims the rays whose impact parameter is at least 0.998 of the
+ * critical one (escaping or orbiting near the photon sphere: the long paths)
+ * first, so the short ones fill the end of the sweep when lanes run out of
+ * work; 0 claims them in index order. Results do not change. */
+void geon_set_sweep_order(int on);
+int geon_get_sweep_order(void);
 /* Device-pointer, stream-ordered forms of the two calls above (alpha, lo, hi and
  * every output are device addresses; the call returns once the work is queued).
  * The bisection keeps its rounds on the device: no host round trip per round. */

@@ -138,6 +138,15 @@ def test_render_batch_argument_errors_without_gpu(lib):
     assert lib.geon_render_batch(items, 1) == -1
 
 
+def test_mixed_null_fix_and_sweep_order_flags_without_gpu(lib):
+    assert lib.geon_get_mixed_null_fix() == 1 and lib.geon_get_sweep_order() == 1  # on by default
+    lib.geon_set_mixed_null_fix(0)
+    lib.geon_set_sweep_order(0)
+    assert lib.geon_get_mixed_null_fix() == 0 and lib.geon_get_sweep_order() == 0
+    lib.geon_set_mixed_null_fix(1)
+    lib.geon_set_sweep_order(1)
+
+
 def test_mixed_orbit_plane_flag_without_gpu(lib):
     assert lib.geon_get_mixed_orbit_plane() == 1  # on by default
     lib.geon_set_mixed_orbit_plane(0)

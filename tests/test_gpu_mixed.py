@@ -52,7 +52,8 @@ def test_mixed_shadow_sweep_matches_fp64(geon):
     assert np.abs(rmx.steps_taken[esc] - r64.steps_taken[esc]).max() <= 1
     # every mixed escape is clean: the mixed path flings no ray off its geodesic
     assert np.array_equal(geon.accuracy.clean_escapes(m, rmx), rmx.termination == 2)
-    assert np.max(rmx.null_residual[esc]) < 1e-6
+    # compensated null re-projection (default on): the FP64 path's null drift
+    assert np.max(rmx.null_residual[esc]) < 1e-11
     _directions_close(m, r64, rmx, 1e-6, 1e-3)
     t, s = geon.shadow.classify(m, 20.0, alpha, 0.01, 200000, precision="mixed")
     assert np.array_equal(t, rmx.termination) and np.array_equal(s, rmx.steps_taken)
@@ -142,6 +143,25 @@ def test_mixed_orbit_plane_opt_out(geon):
     assert not np.array_equal(a.final_state, b.final_state)
     c = geon.trace(m, y0, 0.05, 20000, precision="mixed")
     assert np.array_equal(a.final_state, c.final_state) and np.array_equal(a.termination, c.termination)
+
+
+def test_mixed_null_fix_opt_out(geon):
+    """geon_set_mixed_null_fix(0) leaves p^t to the RK4 alone: the null drift
+    of the FP32 right-hand sides (~1e-8) comes back; classes do not change."""
+    lib = geon._load()
+    assert lib.geon_get_mixed_null_fix() == 1
+    m = geon.Schwarzschild(1.0)
+    alpha = np.radians(np.linspace(15.0, 19.0, 512))
+    on = geon.shadow.trace(m, 20.0, alpha, 0.01, 200000, precision="mixed")
+    lib.geon_set_mixed_null_fix(0)
+    try:
+        off = geon.shadow.trace(m, 20.0, alpha, 0.01, 200000, precision="mixed")
+    finally:
+        lib.geon_set_mixed_null_fix(1)
+    esc = geon.accuracy.clean_escapes(m, on) & geon.accuracy.clean_escapes(m, off)
+    assert esc.sum() > 400
+    assert np.max(on.null_residual[esc]) < 1e-11 < 1e-9 < np.max(off.null_residual[esc])
+    assert np.array_equal(on.termination, off.termination)
 
 
 def test_shadow_dev_api(geon):
