@@ -691,6 +691,18 @@ def config3_leg(geon, lib, n, row_step, check_agreeing=256):
                                       "kind": "port", "sample": f"row 0 ({len(yc)} rays, {dt_cpu:.1f} s)"}}
     out["mixed_ray_steps_per_s_both"] = (sum(out[c]["mixed_total_steps"] for c in cases)
                                          / sum(out[c]["mixed_ms"] / 1e3 for c in cases))
+    # both images in ONE persistent launch (geon_render_batch): the rays of the
+    # two metrics share one work queue; each image must equal its single render
+    cfg = geon.RenderConfig(precision="mixed", show_stars=True)
+    items = [(m, geon.Camera(obs, 90.0, n, n, forward_sign=fwd), cfg) for m, _, _, obs, fwd in cases.values()]
+    singles = [geon.render(m, cam, c, with_classes=True) for m, cam, c in items]
+    dt, res = _wall(lambda: geon.render_batch(items), 1)
+    steps = sum(r[1].total_steps for r in res)
+    out["one_launch_both_images"] = {
+        "ray_steps_per_s": steps / dt, "ms": 1e3 * dt, "total_steps": steps,
+        "images_equal_single_renders": bool(all(np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+                                                for a, b in zip(res, singles))),
+        "api": "geon_render_batch: one trace_multi_mixed_kernel launch over 2 x 2048^2 rays, host wall time"}
     return out
 
 

@@ -302,8 +302,9 @@ int geon_get_mixed_variant(int kind, int source) {
 
 // Autotuner: time every register-cap variant of the mixed kernel on calibration
 // jobs of this metric and keep the fastest per ray source:
-//  source 0 (camera rays; also used for ray arrays): n camera rays of a
-//    60-degree view from the metric's usual observer, step 0.05;
+//  source 0 (camera rays, as the render's trace kernel steps them; also used
+//    for ray arrays): n camera rays of a 60-degree view from the metric's usual
+//    observer, step 0.05;
 //  source 1 (equatorial shadow rays, Schwarzschild only): n launch angles
 //    spread over [10, 20] degrees from r = 20M, step 0.01.
 // Every ray is capped at max_steps. rates_out[3 + 9] receives ray-steps/s per
@@ -324,6 +325,10 @@ static int time_variants(const TraceLaunch& base, int src, int sink, int64_t n, 
     float best_ms = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
       GEON_CUDA(cudaMemsetAsync(L.queue, 0, sizeof(unsigned long long) * 2, s));
+      if (src == SRC_STATE) {  // the states are traced in place: prepare them again, untimed
+        counted();
+        GEON_CUDA(launch_render_prepare(L, s));
+      }
       GEON_CUDA(cudaEventRecord(a, s));
       counted();
       GEON_CUDA(launch_trace_mixed(L, src, sink, s));
@@ -376,8 +381,9 @@ int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, doub
   CameraDesc c;
   if (int rc = make_camera(m, &cam, 1, c, s)) return rc;
   const int64_t n = cam.width * cam.height;
-  DBuf dsrgb, dterm, dsteps, dres, ws, dalpha;
+  DBuf dsrgb, dterm, dsteps, dres, ws, dalpha, dstate;
   GEON_CUDA(dsrgb.alloc(sizeof(float) * 3 * n, s));
+  GEON_CUDA(dstate.alloc(sizeof(uint32_t) * 16 * n, s));
   GEON_CUDA(dterm.alloc(sizeof(int32_t) * n, s));
   GEON_CUDA(dsteps.alloc(sizeof(int64_t) * n, s));
   GEON_CUDA(dres.alloc(sizeof(double) * n, s));
@@ -392,7 +398,9 @@ int geon_autotune_mixed(geon_metric_t m, int64_t n_rays, int64_t max_steps, doub
   L.show_stars = 1;
   L.queue = ws.as<unsigned long long>();
   L.flags = reinterpret_cast<int*>(L.queue + 1);
-  if (int rc = time_variants(L, SRC_CAMERA, SINK_RENDER, n, dsteps.as<int64_t>(), s, rates, &best[0], MIXED_CAPS))
+  L.ystate = dstate.as<uint32_t>();
+  // the trace kernel of the three-kernel render (camera rays prepared, states out)
+  if (int rc = time_variants(L, SRC_STATE, SINK_STATE, n, dsteps.as<int64_t>(), s, rates, &best[0], MIXED_CAPS))
     return rc;
   g_variant[kind][0].store(best[0]);
   if (kind == GEON_SCHWARZSCHILD) {
@@ -657,7 +665,7 @@ static int render_any(geon_metric_t m, const geon_camera* cam, const geon_render
   if (int rc = make_camera(m, cam, spa, c, s)) return rc;
   const int64_t npix = cam->width * cam->height;
   const int64_t nsamp = npix * spa * spa;
-  DBuf dsrgb, dterm, dsteps, dres, drgb, dcls, dpst, ws;
+  DBuf dsrgb, dterm, dsteps, dres, drgb, dcls, dpst, ws, dstate;
   GEON_CUDA(dsrgb.alloc(sizeof(float) * 3 * nsamp, s));
   GEON_CUDA(dterm.alloc(sizeof(int32_t) * nsamp, s));
   GEON_CUDA(dsteps.alloc(sizeof(int64_t) * nsamp, s));
@@ -684,7 +692,15 @@ static int render_any(geon_metric_t m, const geon_camera* cam, const geon_render
   L.queue = wsu;
   L.flags = reinterpret_cast<int*>(wsu + 1);
   unsigned long long* dstats = wsu + 2;  // 6 counters
-  GEON_CUDA(launch_trace(L, cfg->precision, SRC_CAMERA, SINK_RENDER, s));
+  if (cfg->precision == GEON_MIXED) {
+    // prepare / trace / shade (launch_render_mixed): 16 words of state per sample
+    GEON_CUDA(dstate.alloc(sizeof(uint32_t) * 16 * nsamp, s));
+    L.ystate = dstate.as<uint32_t>();
+    counted(3);
+    GEON_CUDA(launch_render_mixed(L, s));
+  } else {
+    GEON_CUDA(launch_trace(L, cfg->precision, SRC_CAMERA, SINK_RENDER, s));
+  }
   counted();
   uint8_t* d8 = rgb8 ? reinterpret_cast<uint8_t*>(dcls.as<int32_t>() + npix) : nullptr;
   GEON_CUDA(launch_render_reduce(dsrgb.as<float>(), dterm.as<int32_t>(), dsteps.as<int64_t>(),
@@ -743,8 +759,11 @@ int geon_render_batch(const geon_render_item* items, size_t n) {
     if (it.render.max_steps < 0) return fail(GEON_ERR_INVALID, "max_steps < 0");
   }
   cudaStream_t s = host_stream();
+  if (precision == GEON_MIXED && (g_reproject.load() || g_band[GEON_SCHWARZSCHILD].load() > 0.0f ||
+                                  g_band[GEON_ALCUBIERRE].load() > 0.0f || g_band[GEON_MORRIS_THORNE].load() > 0.0f))
+    return fail(GEON_ERR_UNSUPPORTED, "geon_render_batch runs the default mixed step (no FP64 band, no re-projection)");
   struct Bufs {
-    DBuf srgb, term, steps, res, rgb, cls, pst;
+    DBuf srgb, term, steps, res, rgb, cls, pst, state;
     int64_t npix = 0, spa = 1;
   };
   std::vector<Bufs> B(n);
@@ -786,6 +805,12 @@ int geon_render_batch(const geon_render_item* items, size_t n) {
     }
     L.queue = wsu;
     L.flags = reinterpret_cast<int*>(wsu + 1);
+    if (precision == GEON_MIXED) {
+      GEON_CUDA(b.state.alloc(sizeof(uint32_t) * 16 * nsamp, s));
+      L.ystate = b.state.as<uint32_t>();
+      counted();
+      GEON_CUDA(launch_render_prepare(L, s));
+    }
     jobs[j] = L;
     D.start[j + 1] = D.start[j] + nsamp;
   }
@@ -800,6 +825,10 @@ int geon_render_batch(const geon_render_item* items, size_t n) {
     const geon_render_item& it = items[j];
     Bufs& b = B[j];
     unsigned long long* dstats = wsu + 2 + 6 * j;
+    if (precision == GEON_MIXED) {
+      counted();
+      GEON_CUDA(launch_render_shade(jobs[j], s));
+    }
     counted();
     GEON_CUDA(launch_render_reduce(b.srgb.as<float>(), b.term.as<int32_t>(), b.steps.as<int64_t>(),
                                    b.res.as<double>(), b.npix, b.spa, b.rgb.as<float>(), b.cls.as<int32_t>(),

@@ -63,9 +63,14 @@ struct GridDesc {
 };
 
 // Sources of initial states.
-enum : int { SRC_ARRAY = 0, SRC_CAMERA = 1, SRC_EQUATORIAL = 2 };
+// SRC_STATE: a stepper state prepared by an earlier kernel (16 words per ray in
+// ystate: the mixed path's (hi, lo) pairs), so the trace kernel itself runs no
+// FP64 set-up code.
+enum : int { SRC_ARRAY = 0, SRC_CAMERA = 1, SRC_EQUATORIAL = 2, SRC_STATE = 3 };
 // Where results go.
-enum : int { SINK_TRACE = 0, SINK_RENDER = 1, SINK_SHADOW = 2 };
+// SINK_STATE: the stepper's final state back into ystate (with term and
+// steps), shaded by a later kernel; the trace kernel runs no FP64 sink code.
+enum : int { SINK_TRACE = 0, SINK_RENDER = 1, SINK_SHADOW = 2, SINK_STATE = 3 };
 
 struct TraceLaunch {
   MetricDesc M;
@@ -77,6 +82,8 @@ struct TraceLaunch {
   int64_t max_steps;
   // SRC_ARRAY
   const double* y0;    // n x 8 (AoS, the reference's State layout)
+  // SRC_STATE / SINK_STATE: 16 words per ray (ray i at ystate + 16 i), in place
+  uint32_t* ystate;
   // SRC_EQUATORIAL (bin/validate_shadow.rs:20-35)
   const double* alpha; // n launch angles
   double r_obs;
@@ -130,6 +137,14 @@ struct MultiDesc {
 };
 cudaError_t launch_trace_multi_fp64(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s);
 cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s);
+// Mixed renders in three kernels (trace_mixed.cu): the camera rays' prepared
+// states into L.ystate, the trace over them (SRC_STATE, SINK_STATE), and the
+// shading of the final states into L.srgb / term / steps / resid (the render
+// sink's outputs). launch_render_mixed runs all three for one job;
+// launch_render_prepare / _shade one end each (several jobs in one trace).
+cudaError_t launch_render_mixed(const TraceLaunch& L, cudaStream_t s);
+cudaError_t launch_render_prepare(const TraceLaunch& L, cudaStream_t s);
+cudaError_t launch_render_shade(const TraceLaunch& L, cudaStream_t s);
 // ---- launchers (trace_fp64fast.cu) ----
 cudaError_t launch_trace_fp64fast(const TraceLaunch& L, int src, int sink, cudaStream_t s);
 // rgb and rgb8 (the tonemapped bytes) may each be null

@@ -73,6 +73,21 @@ __device__ __forceinline__ void load_ray(const TraceLaunch& L, int64_t ray, doub
   }
 }
 
+// A ray's prepared or final stepper state: 16 words, four 16-byte accesses.
+__device__ __forceinline__ void load_words(const TraceLaunch& L, int64_t ray, uint32_t w[16]) {
+  const uint4* p = reinterpret_cast<const uint4*>(L.ystate + 16 * ray);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uint4 v = p[q];
+    w[4 * q] = v.x; w[4 * q + 1] = v.y; w[4 * q + 2] = v.z; w[4 * q + 3] = v.w;
+  }
+}
+__device__ __forceinline__ void store_words(const TraceLaunch& L, int64_t ray, const uint32_t w[16]) {
+  uint4* p = reinterpret_cast<uint4*>(L.ystate + 16 * ray);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) p[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+}
+
 template <int K, int SINK>
 __device__ __forceinline__ void store_ray(const TraceLaunch& L, int64_t ray, int term,
                                           const double y[8], int64_t steps) {
@@ -179,9 +194,15 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
         if (idx < (unsigned long long)L.n) {
           ray = L.order ? (int64_t)L.order[idx] : (int64_t)idx;
           n = 0;
-          double y0[8];
-          load_ray<SRC>(L, ray, y0);
-          st.load(L, y0);
+          if constexpr (SRC == SRC_STATE) {
+            uint32_t w[16];
+            load_words(L, ray, w);
+            st.restore(L, w, 0);
+          } else {
+            double y0[8];
+            load_ray<SRC>(L, ray, y0);
+            st.load(L, y0);
+          }
         }
       }
     }
@@ -191,9 +212,17 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
       int64_t taken = 0;
       n = group_steps(st, L, L.max_steps, n, t, taken);
       if (t != TERM_NONE) {
-        double y[8];
-        st.to_double(y);
-        store_ray<K, SINK>(L, ray, t, y, taken);
+        if constexpr (SINK == SINK_STATE) {
+          uint32_t w[16];
+          st.save(w);
+          store_words(L, ray, w);
+          L.term[ray] = t;
+          L.steps[ray] = taken;
+        } else {
+          double y[8];
+          st.to_double(y);
+          store_ray<K, SINK>(L, ray, t, y, taken);
+        }
         ray = -1;
       }
     }
@@ -251,10 +280,17 @@ __device__ __forceinline__ void trace_loop_multi(const TraceLaunch* __restrict__
           ray = (int64_t)idx - D.start[j];
           n = 0;
           const TraceLaunch& L = jobs[j];
-          double y0[8];
-          load_ray<SRC>(L, ray, y0);
-          st.bind(L, SRC);
-          st.load(L, y0);
+          if constexpr (SRC == SRC_STATE) {
+            uint32_t w[16];
+            load_words(L, ray, w);
+            st.bind(L, SRC_CAMERA);  // prepared camera rays
+            st.restore(L, w, 0);
+          } else {
+            double y0[8];
+            load_ray<SRC>(L, ray, y0);
+            st.bind(L, SRC);
+            st.load(L, y0);
+          }
         }
       }
     }
@@ -265,9 +301,17 @@ __device__ __forceinline__ void trace_loop_multi(const TraceLaunch* __restrict__
       int64_t taken = 0;
       n = group_steps(st, L, L.max_steps, n, t, taken);
       if (t != TERM_NONE) {
-        double y[8];
-        st.to_double(y);
-        store_ray_any<SINK>(L, L.M.kind, ray, t, y, taken);
+        if constexpr (SINK == SINK_STATE) {
+          uint32_t w[16];
+          st.save(w);
+          store_words(L, ray, w);
+          L.term[ray] = t;
+          L.steps[ray] = taken;
+        } else {
+          double y[8];
+          st.to_double(y);
+          store_ray_any<SINK>(L, L.M.kind, ray, t, y, taken);
+        }
         job = -1;
       }
     }

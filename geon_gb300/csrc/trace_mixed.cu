@@ -640,9 +640,11 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
 // One persistent kernel over the rays of several renders (any metric kinds):
 // the default mixed step per ray, camera rays of the spherically symmetric
 // metrics in their orbit plane when the orbit-plane option is on (as in the
-// single-render kernels, so each image equals its single render).
-__global__ void __launch_bounds__(TRACE_BLOCK, 5) trace_multi_mixed_kernel(const TraceLaunch* jobs, const MultiDesc D) {
-  trace_loop_multi<MixedStepperAny<FEAT_ORBIT_DYN>, SRC_CAMERA, SINK_RENDER>(jobs, D);
+// single-render kernels, so each image equals its single render). The rays'
+// states are prepared and shaded per render by the three-kernel render's
+// prepare and shade kernels.
+__global__ void __launch_bounds__(TRACE_BLOCK) trace_multi_mixed_kernel(const TraceLaunch* jobs, const MultiDesc D) {
+  trace_loop_multi<MixedStepperAny<FEAT_ORBIT_DYN>, SRC_STATE, SINK_STATE>(jobs, D);
 }
 
 cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s) {
@@ -702,7 +704,90 @@ template <int K>
 static cudaError_t launch_mk(const TraceLaunch& L, int src, int sink, cudaStream_t s) {
   if (src == SRC_ARRAY && sink == SINK_TRACE) return launch_mst<K, SRC_ARRAY, SINK_TRACE>(L, s);
   if (src == SRC_CAMERA && sink == SINK_RENDER) return launch_mst<K, SRC_CAMERA, SINK_RENDER>(L, s);
+  if (src == SRC_STATE && sink == SINK_STATE) return launch_mst<K, SRC_STATE, SINK_STATE>(L, s);
   return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed renders in three kernels. The trace kernel of a render spends almost
+// all its time in the FP32 step, but its FP64 set-up and sink code (the camera
+// ray, the orbit-plane frame, the null residual, the escape direction, the sky)
+// sets its register count and so its occupancy. Here the set-up runs in a
+// prepare kernel (camera ray -> the stepper's (hi, lo) state, 16 words per ray
+// in L.ystate), the trace kernel steps those states and writes the final ones
+// back in place, and a shade kernel turns them into the render sink's outputs.
+// Every value is computed by the same stepper code as in the one-kernel
+// render, so the results are the same bits.
+// ---------------------------------------------------------------------------
+template <int K, int FEAT>
+__global__ void __launch_bounds__(128) render_prepare_kernel(const TraceLaunch L) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.n) return;
+  double y0[8];
+  camera_ray(L.cam, i, y0);
+  MixedStepper<K, FEAT> st;
+  st.load(L, y0);
+  uint32_t w[16];
+  st.save(w);
+  store_words(L, i, w);
+}
+
+template <int K, int FEAT>
+__global__ void __launch_bounds__(128) render_shade_kernel(const TraceLaunch L) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.n) return;
+  uint32_t w[16];
+  load_words(L, i, w);
+  const int64_t steps = L.steps[i];
+  MixedStepper<K, FEAT> st;
+  st.restore(L, w, steps);
+  st.resume_frame(L, i);
+  double y[8];
+  st.to_double(y);
+  store_ray<K, SINK_RENDER>(L, i, L.term[i], y, steps);
+}
+
+// the orbit-plane frame applies to this render's rays (as in launch_mst)
+static bool render_orbit(const TraceLaunch& L) {
+  return (L.M.kind == KIND_SCHWARZSCHILD || L.M.kind == KIND_MORRIS_THORNE) && (L.mixed_flags & MIXED_ORBIT) &&
+         !(L.band > 0.0f) && !(L.mixed_flags & MIXED_REPROJECT);
+}
+
+template <int K, int FEAT>
+static cudaError_t launch_prepare_shade(const TraceLaunch& L, bool prepare, cudaStream_t s) {
+  const unsigned grid = (unsigned)((L.n + 127) / 128);
+  if (prepare) render_prepare_kernel<K, FEAT><<<grid, 128, 0, s>>>(L);
+  else render_shade_kernel<K, FEAT><<<grid, 128, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+static cudaError_t prepare_or_shade(const TraceLaunch& L, bool prepare, cudaStream_t s) {
+  if (L.n <= 0) return cudaSuccess;
+  const bool orbit = render_orbit(L);
+  switch (L.M.kind) {
+    case KIND_MINKOWSKI: return launch_prepare_shade<KIND_MINKOWSKI, 0>(L, prepare, s);
+    case KIND_SCHWARZSCHILD:
+      return orbit ? launch_prepare_shade<KIND_SCHWARZSCHILD, FEAT_ORBIT>(L, prepare, s)
+                   : launch_prepare_shade<KIND_SCHWARZSCHILD, 0>(L, prepare, s);
+    case KIND_ALCUBIERRE: return launch_prepare_shade<KIND_ALCUBIERRE, 0>(L, prepare, s);
+    case KIND_MORRIS_THORNE:
+      return orbit ? launch_prepare_shade<KIND_MORRIS_THORNE, FEAT_ORBIT>(L, prepare, s)
+                   : launch_prepare_shade<KIND_MORRIS_THORNE, 0>(L, prepare, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_render_prepare(const TraceLaunch& L, cudaStream_t s) { return prepare_or_shade(L, true, s); }
+cudaError_t launch_render_shade(const TraceLaunch& L, cudaStream_t s) { return prepare_or_shade(L, false, s); }
+
+cudaError_t launch_render_mixed(const TraceLaunch& L, cudaStream_t s) {
+  if (L.n <= 0) return cudaSuccess;
+  if (L.band > 0.0f || (L.mixed_flags & MIXED_REPROJECT))  // the chart options keep the one-kernel render
+    return launch_trace_mixed(L, SRC_CAMERA, SINK_RENDER, s);
+  cudaError_t e = launch_render_prepare(L, s);
+  if (e == cudaSuccess) e = launch_trace_mixed(L, SRC_STATE, SINK_STATE, s);
+  if (e == cudaSuccess) e = launch_render_shade(L, s);
+  return e;
 }
 
 cudaError_t launch_trace_mixed(const TraceLaunch& L, int src, int sink, cudaStream_t s) {
