@@ -111,12 +111,16 @@ __device__ __forceinline__ void rhs_planar(const AConsts<float>& C, float r, flo
     *k7 = (u * q) * p3;
     return;
   }
-  const float ir = Mt::rcp(r);
-  const float f = Mt::fma(-C.two_m, ir, 1.0f);
-  const float A = C.m * ir * ir;
-  const float gtr = Mt::div(A, f);
+  // One reciprocal, of D = r (r - 2M): Gamma^t_tr = M / (r^2 f) = M / D,
+  // 1/r = (r - 2M) / D, f = (r - 2M) / r, and Gamma^r_tt = M f / r^2 =
+  // Gamma^t_tr f^2, so the p^t^2 and p^r^2 terms share the factor Gamma^t_tr.
+  const float rm = r - C.two_m;
+  const float iD = Mt::rcp(r * rm);
+  const float gtr = C.m * iD;
+  const float ir = rm * iD;
+  const float E = (rm * ir) * p0;  // f p^t
   *k4 = (u * gtr) * p0;
-  *k5 = Mt::fma(-A * f, p0 * p0, Mt::fma(gtr, p1 * p1, (r - C.two_m) * (p3 * p3)));
+  *k5 = Mt::fma(gtr, Mt::fma(-E, E, p1 * p1), rm * (p3 * p3));
   *k7 = (u * ir) * p3;
 }
 
