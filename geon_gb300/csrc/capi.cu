@@ -1091,6 +1091,7 @@ int geon_shadow_bisect_dev(geon_metric_t m, double r_obs, const double* lo, cons
     T.steps = tsteps.as<int64_t>();
     T.queue = ws.as<unsigned long long>();
     T.flags = reinterpret_cast<int*>(T.queue + 1);
+    T.decide = 1;  // only each ray's class matters to the walk
     GEON_CUDA(launch_trace(T, precision, SRC_EQUATORIAL, SINK_SHADOW, s));
     counted();
     GEON_CUDA(launch_bisect_walk((int64_t)nb, per, L, tree.as<double>(), tterm.as<int32_t>(),

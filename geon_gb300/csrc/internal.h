@@ -102,6 +102,8 @@ struct TraceLaunch {
   float reserve_per_sm;  // persistent grid leaves this many blocks per SM free (may be fractional)
   int variant;         // mixed kernel register-cap variant (0: none, 1: 8 blocks/SM, 2: 10)
   int mixed_flags;     // MIXED_* bits
+  int decide;          // shadow rays whose class is all a caller needs (bisection rounds): the mixed
+                       // path ends a ray as soon as its class is settled (MixedCore::decided_k)
   // adaptive stepping (GEON_ADAPTIVE): error tolerances
   double rtol, atol;
   // work queue

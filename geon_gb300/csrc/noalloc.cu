@@ -129,6 +129,7 @@ extern "C" int geon_shadow_bisect_dev_noalloc(geon_metric_t m, double r_obs, con
     T.steps = tsteps;
     T.queue = queue;
     T.flags = reinterpret_cast<int*>(queue + 1);
+    T.decide = 1;  // as geon_shadow_bisect_dev: only each ray's class matters
     NOALLOC_CUDA(launch_trace_any(T, precision, SRC_EQUATORIAL, SINK_SHADOW, s));
     NOALLOC_CUDA(launch_bisect_walk((int64_t)nb, per, L, tree, tterm, tsteps, wlo, whi, wst, s));
     note_launches(3);

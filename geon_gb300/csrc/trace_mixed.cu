@@ -91,8 +91,10 @@ __device__ __forceinline__ bool ff_gt(float hi, float lo, float thi, float tlo) 
 // (Schwarzschild, Morris-Thorne) are turned into the frame of their own orbit
 // plane at load, stepped there on the equator, and turned back at the end;
 // FEAT_ORBIT_DYN: a per-ray flag says so (the serving kernel: camera rays).
+// FEAT_DECIDE: every ray is a bisection ray whose class settles early
+// (decided_k); FEAT_DECIDE_DYN: a per-ray flag says so (the serving kernel).
 enum : int { FEAT_BAND = 1, FEAT_REPROJECT = 2, FEAT_PLANAR = 4, FEAT_PLANAR_DYN = 8, FEAT_ORBIT = 16,
-             FEAT_ORBIT_DYN = 32 };
+             FEAT_ORBIT_DYN = 32, FEAT_DECIDE = 64, FEAT_DECIDE_DYN = 128 };
 
 // Right-hand side on the equatorial plane: rhs_stage at sin theta = 1,
 // cos theta = 0, p^theta = 0, where its theta terms vanish (Gamma^th_phph =
@@ -135,6 +137,8 @@ struct MixedCore {
   bool ready = false;
   bool planar = (FEAT & FEAT_PLANAR) != 0;
   bool orbit = (FEAT & FEAT_ORBIT) != 0;
+  bool decide = (FEAT & FEAT_DECIDE) != 0;
+  float cap_steps;  // the step cap (max_steps), for the early decision's budget test
   float oe1[3], oe2[3];  // orbit-plane frame (FEAT_ORBIT, FEAT_ORBIT_DYN)
   // rays of metric kind K can step in their orbit-plane frame
   template <int K>
@@ -147,6 +151,7 @@ struct MixedCore {
   __device__ __forceinline__ void set_source(int src) {
     if (FEAT & FEAT_PLANAR_DYN) planar = src == SRC_EQUATORIAL;
     if (FEAT & FEAT_ORBIT_DYN) orbit = src == SRC_CAMERA;
+    if (FEAT & FEAT_DECIDE_DYN) decide = src == SRC_EQUATORIAL;  // served bisection rays
   }
   // Serving: a resumed camera ray gets its orbit-plane frame back from its
   // initial state (the frame is a function of it, so it is the one the ray
@@ -173,6 +178,7 @@ struct MixedCore {
     h = (float)L.step;
     hh = (float)L.half_step;
     sixth = (float)L.sixth;
+    cap_steps = (float)L.max_steps;
     ready = true;
   }
 
@@ -214,6 +220,29 @@ struct MixedCore {
     for (int i = 0; i < 8; ++i) out[i] = y[i];
   }
 
+  // Early decision for bisection rays (validate_shadow.rs:37-41 needs only
+  // whether a ray is captured). In Schwarzschild a null geodesic has at most one
+  // turning point, outside the photon sphere r = 3M: a ray moving outward
+  // beyond it (here r > 3.3M, p^r > 0) has passed its turning point and reaches
+  // the escape radius, and p^r only grows on the way, so it gets there within
+  // (r_esc - r) / p^r of affine parameter; if that fits in the steps left
+  // before the cap (2 % margin) the ray is reported Escaped now. A ray moving
+  // inward inside the photon sphere (r < 2.9M, p^r < 0) has no turning point
+  // left and is reported Captured now. The class is the one the full trace
+  // would end with; steps_taken counts the steps actually taken.
+  template <int K>
+  __device__ __forceinline__ int decided_k() const {
+    if (K == KIND_SCHWARZSCHILD) {
+      if (hi[5] > 0.0f) {
+        if (hi[1] > 3.3f * C.m && (esc_hi - hi[1]) * 1.02f < (cap_steps - (float)nsteps - 2.0f) * h * hi[5])
+          return TERM_ESCAPED;
+      } else if (hi[1] < 2.9f * C.m) {
+        return TERM_CAPTURED;
+      }
+    }
+    return TERM_NONE;
+  }
+
   // Termination tests of the reference, evaluated on the compensated state.
   template <int K>
   __device__ __forceinline__ int terminate_k(const TraceLaunch&) const {
@@ -221,7 +250,12 @@ struct MixedCore {
       if (!isfinite(hi[1])) return TERM_DIVERGED;
       // Far from both radii the high word decides: |lo| stays below 2^-20 of
       // hi between renormalisations, far inside the 2^-10 margins.
-      if (hi[1] > cap_far && hi[1] < esc_far) return TERM_NONE;
+      if (hi[1] > cap_far && hi[1] < esc_far) {
+        if constexpr ((FEAT & (FEAT_DECIDE | FEAT_DECIDE_DYN)) != 0) {
+          if (decide) return decided_k<K>();
+        }
+        return TERM_NONE;
+      }
       if (ff_gt(cap_hi, cap_lo, hi[1], lo[1])) return TERM_CAPTURED;
       if (ff_gt(hi[1], lo[1], esc_hi, esc_lo)) return TERM_ESCAPED;
       return TERM_NONE;
@@ -619,6 +653,7 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
     case FEAT_BAND | FEAT_REPROJECT: return launch_mst_v<K, SRC, SINK, 1, FEAT_BAND | FEAT_REPROJECT>(L, s);
   }
   if constexpr (SRC == SRC_EQUATORIAL && SINK == SINK_SHADOW) {
+    if (L.decide) return launch_mst_v<K, SRC, SINK, 1, FEAT_DECIDE>(L, s);  // bisection rounds
     // variant = register cap + 3 * block size (128, 64, 256); the same caps in
     // registers per thread (64, 51) at every block size
     switch (L.variant) {
@@ -676,7 +711,7 @@ cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D
 template <int K>
 __global__ void __launch_bounds__(TRACE_BLOCK, 7) serve_mixed_kernel(const ServeJob* jobs, ServeCounters cnt,
                                                                      ServeClass* cl, const unsigned* epoch, int budget) {
-  constexpr int F = K == KIND_SCHWARZSCHILD ? (FEAT_PLANAR_DYN | FEAT_ORBIT_DYN)
+  constexpr int F = K == KIND_SCHWARZSCHILD ? (FEAT_PLANAR_DYN | FEAT_ORBIT_DYN | FEAT_DECIDE_DYN)
                     : K == KIND_MORRIS_THORNE ? FEAT_ORBIT_DYN : 0;
   serve_loop<MixedStepper<K, F>, K>(jobs, cnt, cl, epoch, budget);
 }

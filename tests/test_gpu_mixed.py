@@ -66,6 +66,25 @@ def test_mixed_bisection_b_c(geon):
     assert abs(b_c - 3.0 * np.sqrt(3.0)) / (3.0 * np.sqrt(3.0)) <= 1e-6
 
 
+def test_mixed_bisection_early_decision_equals_full_traces(geon):
+    """Bisection rounds of the mixed path end a ray as soon as its class is
+    settled (outward beyond 3.3M with the escape radius within the steps left,
+    or inward inside 2.9M); the halvings must be the ones the full traces give
+    (geon_shadow_classify runs each ray to its end)."""
+    m = geon.Schwarzschild(1.0)
+    lo0 = np.radians([13.1, 13.6, 14.0, 14.2])
+    hi0 = np.radians([14.9, 15.3, 14.5, 14.35])
+    lo, hi = lo0.copy(), hi0.copy()
+    for _ in range(24):  # bin/validate_shadow.rs:70-77, all brackets at once
+        mid = 0.5 * (lo + hi)
+        cap = geon.shadow.is_captured(m, 20.0, mid, precision="mixed")
+        lo = np.where(cap, mid, lo)
+        hi = np.where(cap, hi, mid)
+    ac, lo_b, hi_b, st = geon.shadow.bisect(m, 20.0, lo0, hi0, iters=24, precision="mixed")
+    assert np.array_equal(lo_b, lo) and np.array_equal(hi_b, hi)
+    assert np.array_equal(ac, 0.5 * (lo + hi))
+
+
 def test_mixed_render_schwarzschild(geon):
     """BASELINE config-1 view (r 30M, fov 60, h 0.05, cap 20000, escape 100M) at 128^2."""
     m = geon.Schwarzschild(1.0, 1.001, 100.0)
