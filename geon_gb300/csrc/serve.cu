@@ -258,7 +258,7 @@ cudaError_t publish(geon_server* S, HostJob* J, const ServeJob& sj) {
   const int slot = J->slot;
   S->h_jobs[slot] = sj;
   S->h_jobs[slot].L.band = 0.0f;  // served mixed requests use the default mixed step
-  S->h_jobs[slot].L.mixed_flags = 0;
+  S->h_jobs[slot].L.mixed_flags = SERVE_MIXED_FLAGS;
   cudaError_t e = cudaMemcpyAsync(S->d_jobs + slot, S->h_jobs + slot, sizeof sj, cudaMemcpyHostToDevice, S->s_main);
   for (int k = 0; k < 3 && e == cudaSuccess; ++k)
     e = cudaMemsetAsync(S->d_counters + (size_t)k * SERVE_MAX_JOBS + slot, 0, sizeof(unsigned long long), S->s_main);
@@ -299,7 +299,6 @@ cudaError_t bisect_publish_round(geon_server* S, HostJob* J) {
   ServeJob sj;
   std::memset(&sj, 0, sizeof sj);
   sj.L = trace_launch_defaults(J->metric, J->spec.step, J->spec.max_steps);
-  sj.L.mixed_flags = SERVE_MIXED_FLAGS;
   sj.L.n = J->nrays;
   sj.L.alpha = b.alpha;
   sj.L.r_obs = J->spec.r_obs;
@@ -342,7 +341,6 @@ int start_job(geon_server* S, HostJob* J) {
     ServeJob sj;
     std::memset(&sj, 0, sizeof sj);
     sj.L = trace_launch_defaults(J->metric, q.render.step, q.render.max_steps);
-    sj.L.mixed_flags = SERVE_MIXED_FLAGS;
     sj.L.cam = c;
     sj.L.n = J->nsamp;
     sj.L.srgb = b.srgb;
