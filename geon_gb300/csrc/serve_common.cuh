@@ -185,6 +185,7 @@ __device__ __forceinline__ void serve_loop(const ServeJob* __restrict__ jobs, Se
           break;
         }
       }
+      if (slot >= 0) st.group_end(L);  // the ray survived a whole group of TRACE_INNER steps
     }
   }
   if (slot >= 0) {  // out of budget: park the ray for the next launch

@@ -130,6 +130,7 @@ struct AdaptiveStepper {
     }
     return STEP_NONFINITE;
   }
+  __device__ __forceinline__ void group_end(const TraceLaunch&) {}
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
   }

@@ -165,6 +165,7 @@ __device__ __forceinline__ int64_t group_steps(Stepper& st, const TraceLaunch& L
   }
   n += done;
   taken = n + extra;
+  if (t == TERM_NONE) st.group_end(L);  // the ray survived a whole group of TRACE_INNER steps
   return n;
 }
 

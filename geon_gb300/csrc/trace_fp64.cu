@@ -39,6 +39,7 @@ struct Fp64Stepper {
     for (int i = 0; i < 8; ++i) y[i] = yn[i];
     return STEP_OK;
   }
+  __device__ __forceinline__ void group_end(const TraceLaunch&) {}
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
   }
@@ -103,6 +104,7 @@ struct Fp64StepperAny {
     for (int i = 0; i < 8; ++i) y[i] = yn[i];
     return STEP_OK;
   }
+  __device__ __forceinline__ void group_end(const TraceLaunch&) {}
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
   }

@@ -200,6 +200,7 @@ struct FastSchwStepper {
     for (int i = 0; i < 8; ++i) y[i] = yn[i];
     return STEP_OK;
   }
+  __device__ __forceinline__ void group_end(const TraceLaunch&) {}
   __device__ __forceinline__ void finish(const TraceLaunch&) {}
 };
 

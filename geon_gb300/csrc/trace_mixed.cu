@@ -23,30 +23,26 @@
 
 namespace geon {
 
-// (hi, lo) += inc, compensated. The rounding error of hi + inc is recovered
-// exactly (TwoSum, Knuth; or Fast2Sum, Dekker, when |hi| >= |inc| is known) and
-// accumulated into lo; hi is not renormalised here (see renormalise()).
+// (hi, lo) += inc, compensated: the low word is folded into the increment and
+// the rounding error of hi + (inc + lo) becomes the new low word (TwoSum,
+// Knuth; or Fast2Sum, Dekker, when |hi| >= |inc + lo| is known). hi stays the
+// FP32 number nearest to hi + lo (|lo| <= ulp(hi)/2), so the stages, which
+// are evaluated at the high words, see the state to FP32 precision, and no
+// separate renormalisation is needed; the value lost per step is the rounding
+// of inc + lo, 2^-24 of the increment, below the FP32 evaluation error of the
+// increment itself.
 __device__ __forceinline__ void two_sum_update(float& hi, float& lo, float inc) {
-  const float s = hi + inc;
+  const float t = inc + lo;
+  const float s = hi + t;
   const float bb = s - hi;
-  const float e = (hi - (s - bb)) + (inc - bb);
-  lo = lo + e;
+  lo = (hi - (s - bb)) + (t - bb);
   hi = s;
 }
 
 __device__ __forceinline__ void fast_two_sum_update(float& hi, float& lo, float inc) {
-  const float s = hi + inc;
-  const float e = (hi - s) + inc;
-  lo = lo + e;
-  hi = s;
-}
-
-// Fold lo back into hi so that |lo| <= ulp(hi)/2 again (Fast2Sum). Between
-// renormalisations |lo| grows by at most ulp(hi)/2 per step, so every 8 steps
-// keeps its own rounding far below the FP32 evaluation error of the RHS.
-__device__ __forceinline__ void renormalise(float& hi, float& lo) {
-  const float s = hi + lo;
-  lo = lo - (s - hi);
+  const float t = inc + lo;
+  const float s = hi + t;
+  lo = (hi - s) + t;
   hi = s;
 }
 
@@ -133,7 +129,7 @@ struct MixedCore {
   float cap_hi, cap_lo, esc_hi, esc_lo;
   float cap_far, esc_far;  // cap_hi (1 + 2^-10), esc_hi (1 - 2^-10)
   float h, hh, sixth;
-  unsigned nsteps = 0;  // steps this ray has taken: renormalisation follows the ray, not the lane
+  unsigned nsteps = 0;  // steps this ray has taken (counted where the early decision needs it)
   bool ready = false;
   bool planar = (FEAT & FEAT_PLANAR) != 0;
   bool orbit = (FEAT & FEAT_ORBIT) != 0;
@@ -243,13 +239,31 @@ struct MixedCore {
     return TERM_NONE;
   }
 
+  // The step count of the ray, kept only where the early decision reads it.
+  __device__ __forceinline__ void count_step() {
+    if constexpr ((FEAT & (FEAT_DECIDE | FEAT_DECIDE_DYN)) != 0) ++nsteps;
+  }
+
+  // After every group of 16 steps a ray survives (rays start at a warp refill
+  // and refills come every 16 steps, so this is the same step of every lane of
+  // the warp, and every 16th step of each ray): the compensated null
+  // re-projection of a ray stepping on its plane.
+  template <int K>
+  __device__ __forceinline__ void group_end_k(const TraceLaunch& L) {
+    if (!(L.mixed_flags & MIXED_NULLFIX)) return;
+    const bool on_plane = (any_orbit<K>() && orbit) ||
+                          (K == KIND_SCHWARZSCHILD && (FEAT & (FEAT_PLANAR | FEAT_PLANAR_DYN)) != 0 &&
+                           ((FEAT & FEAT_PLANAR) != 0 || planar));
+    if (on_plane) null_fix_planar<K>();
+  }
+
   // Termination tests of the reference, evaluated on the compensated state.
   template <int K>
   __device__ __forceinline__ int terminate_k(const TraceLaunch&) const {
     if (K == KIND_SCHWARZSCHILD) {
       if (!isfinite(hi[1])) return TERM_DIVERGED;
-      // Far from both radii the high word decides: |lo| stays below 2^-20 of
-      // hi between renormalisations, far inside the 2^-10 margins.
+      // Far from both radii the high word decides: |lo| <= ulp(hi)/2 = 2^-24
+      // of hi, far inside the 2^-10 margins.
       if (hi[1] > cap_far && hi[1] < esc_far) {
         if constexpr ((FEAT & (FEAT_DECIDE | FEAT_DECIDE_DYN)) != 0) {
           if (decide) return decided_k<K>();
@@ -368,10 +382,7 @@ struct MixedCore {
     }
 #pragma unroll
     for (int i = 4; i < 8; ++i) two_sum_update(hi[i], lo[i], inc[i]);
-    if ((++nsteps & 7) == 0) {
-#pragma unroll
-      for (int i = 0; i < 8; ++i) renormalise(hi[i], lo[i]);
-    }
+    count_step();
     if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT)) {
       float s = 0.0f;
       if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) s = sinf(hi[2]);
@@ -389,7 +400,7 @@ struct MixedCore {
   // ray in its orbit-plane frame; Morris-Thorne in its orbit-plane frame): the
   // six components that move (t, r or l, phi and their momenta), theta and
   // p^theta held at their loaded values (pi/2 and 0). Same stage points,
-  // horizon rule, compensated update and renormalisation as step_fp32.
+  // horizon rule and compensated update as step_fp32.
   template <int K>
   __device__ __forceinline__ int step_fp32_planar_k(const TraceLaunch& L) {
     float k1, k4, k5, k7;
@@ -439,17 +450,7 @@ struct MixedCore {
     fast_two_sum_update(hi[4], lo[4], i4);
     two_sum_update(hi[5], lo[5], i5);
     fast_two_sum_update(hi[7], lo[7], i7);
-    if ((++nsteps & 7) == 0) {
-      renormalise(hi[0], lo[0]);
-      renormalise(hi[1], lo[1]);
-      renormalise(hi[3], lo[3]);
-      renormalise(hi[4], lo[4]);
-      renormalise(hi[5], lo[5]);
-      renormalise(hi[7], lo[7]);
-      // every 16 steps of the ray: the same step of every lane of a warp (rays
-      // start at a refill, refills come every 16 steps), so warp-uniform
-      if ((nsteps & 15) == 0 && (L.mixed_flags & MIXED_NULLFIX)) null_fix_planar<K>();
-    }
+    count_step();
     if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT)) {
       const float x[4] = {hi[0], hi[1], hi[2], hi[3]};
       const float p[4] = {hi[4], hi[5], 0.0f, hi[7]};
@@ -502,7 +503,7 @@ struct MixedCore {
     }
     if (!finite) return STEP_NONFINITE;
     load_state(yn);
-    ++nsteps;
+    count_step();
     return STEP_OK;
   }
 
@@ -549,6 +550,7 @@ struct MixedStepper : MixedCore<FEAT> {
   __device__ __forceinline__ void to_double(double out[8]) const { this->template to_double_k<K>(out); }
   __device__ __forceinline__ int terminate(const TraceLaunch& L) const { return this->template terminate_k<K>(L); }
   __device__ __forceinline__ int step(const TraceLaunch& L) { return this->template step_k<K>(L); }
+  __device__ __forceinline__ void group_end(const TraceLaunch& L) { this->template group_end_k<K>(L); }
 };
 
 // The stepper of a launch whose rays have different metric kinds (several
@@ -595,6 +597,13 @@ struct MixedStepperAny : MixedCore<FEAT> {
       case KIND_MORRIS_THORNE: return this->template step_k<KIND_MORRIS_THORNE>(L);
       case KIND_ALCUBIERRE: return this->template step_k<KIND_ALCUBIERRE>(L);
       default: return this->template step_k<KIND_MINKOWSKI>(L);
+    }
+  }
+  __device__ __forceinline__ void group_end(const TraceLaunch& L) {
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: this->template group_end_k<KIND_SCHWARZSCHILD>(L); return;
+      case KIND_MORRIS_THORNE: this->template group_end_k<KIND_MORRIS_THORNE>(L); return;
+      default: return;
     }
   }
 };
