@@ -143,29 +143,26 @@ __device__ __forceinline__ int64_t group_steps(Stepper& st, const TraceLaunch& L
   const int64_t left64 = max_steps - n;
   const int left = left64 < (int64_t)TRACE_INNER ? (int)left64 : TRACE_INNER;
   int done = 0, extra = 0;
+  t = TERM_NONE;
 #pragma unroll 1
-  for (int inner = 0; inner < TRACE_INNER; ++inner) {
-    if (done >= left) {  // loop exhausted: Diverged with steps_taken = max_steps
-      t = TERM_DIVERGED;
-      break;
-    }
+  for (; done < left; ++done) {
     t = st.terminate(L);
     if (t != TERM_NONE) break;
     const int r = st.step(L);
-    if (r == STEP_OK) {
-      ++done;
-    } else if (r == STEP_NONFINITE) {
-      t = TERM_DIVERGED;  // NaN guard: keep the pre-step state
-      break;
-    } else {
-      t = TERM_CAPTURED;
-      extra = 1;
+    if (r != STEP_OK) {
+      // NaN guard: Diverged with the pre-step state; horizon step: Captured
+      // with one more step counted
+      t = r == STEP_NONFINITE ? TERM_DIVERGED : TERM_CAPTURED;
+      extra = r == STEP_NONFINITE ? 0 : 1;
       break;
     }
   }
   n += done;
   taken = n + extra;
-  if (t == TERM_NONE) st.group_end(L);  // the ray survived a whole group of TRACE_INNER steps
+  if (t == TERM_NONE) {
+    if (done == TRACE_INNER) st.group_end(L);  // the ray survived a whole group of TRACE_INNER steps
+    if (n >= max_steps) t = TERM_DIVERGED;     // loop exhausted: steps_taken = max_steps
+  }
   return n;
 }
 

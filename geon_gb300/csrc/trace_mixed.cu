@@ -261,15 +261,15 @@ struct MixedCore {
   template <int K>
   __device__ __forceinline__ int terminate_k(const TraceLaunch&) const {
     if (K == KIND_SCHWARZSCHILD) {
-      if (!isfinite(hi[1])) return TERM_DIVERGED;
       // Far from both radii the high word decides: |lo| <= ulp(hi)/2 = 2^-24
-      // of hi, far inside the 2^-10 margins.
+      // of hi, far inside the 2^-10 margins. (A non-finite r fails this test.)
       if (hi[1] > cap_far && hi[1] < esc_far) {
         if constexpr ((FEAT & (FEAT_DECIDE | FEAT_DECIDE_DYN)) != 0) {
           if (decide) return decided_k<K>();
         }
         return TERM_NONE;
       }
+      if (!isfinite(hi[1])) return TERM_DIVERGED;
       if (ff_gt(cap_hi, cap_lo, hi[1], lo[1])) return TERM_CAPTURED;
       if (ff_gt(hi[1], lo[1], esc_hi, esc_lo)) return TERM_ESCAPED;
       return TERM_NONE;
