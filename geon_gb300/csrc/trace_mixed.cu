@@ -128,6 +128,7 @@ struct MixedCore {
   AConsts<float> C;
   float cap_hi, cap_lo, esc_hi, esc_lo;
   float cap_far, esc_far;  // cap_hi (1 + 2^-10), esc_hi (1 - 2^-10)
+  float r_near;             // 3M (1.5 * 2M): inside it the horizon rules can apply
   float h, hh, sixth;
   unsigned nsteps = 0;  // steps this ray has taken (counted where the early decision needs it)
   bool ready = false;
@@ -170,6 +171,7 @@ struct MixedCore {
     esc_hi = __double2float_rn(L.M.escape_r);
     esc_lo = __double2float_rn(L.M.escape_r - (double)esc_hi);
     cap_far = cap_hi * (1.0f + 0x1p-10f);
+    r_near = 1.5f * C.two_m;
     esc_far = esc_hi * (1.0f - 0x1p-10f);
     h = (float)L.step;
     hh = (float)L.half_step;
@@ -325,7 +327,7 @@ struct MixedCore {
   // Captured there instead. Elsewhere |increment / p^t| = 2 M h |p^r| / (r^2 f)
   // stays far below a quarter at any sensible step.
   __device__ __forceinline__ bool unresolved_infall(float inc_pt) const {
-    return hi[5] < 0.0f && hi[1] < 1.5f * C.two_m && !(fabsf(inc_pt) < 0.25f * hi[4]);
+    return hi[5] < 0.0f && hi[1] < r_near && !(fabsf(inc_pt) < 0.25f * hi[4]);
   }
 
   // Returns STEP_OK, STEP_NONFINITE (state unchanged) or STEP_HORIZON: an RK4
@@ -429,10 +431,15 @@ struct MixedCore {
         a7 = __fmaf_rn(2.0f, k7, a7);
       }
     }
-    if (K == KIND_SCHWARZSCHILD && !(rmin > C.two_m)) return STEP_HORIZON;
     const float i0 = sixth * (a0 + k0), i1 = sixth * (a1 + k1), i3 = sixth * (a3 + k3);
     const float i4 = sixth * (a4 + k4), i5 = sixth * (a5 + k5), i7 = sixth * (a7 + k7);
-    if (K == KIND_SCHWARZSCHILD && unresolved_infall(i4)) return STEP_HORIZON;
+    // The horizon rules (a stage at or inside 2M; an unresolved infall, which
+    // needs r < 3M) are tested only when a stage or the ray is within 3M (or a
+    // stage radius is not a number): one test per step far from the hole.
+    if (K == KIND_SCHWARZSCHILD && (!(rmin > r_near) || hi[1] < r_near)) {
+      if (!(rmin > C.two_m)) return STEP_HORIZON;
+      if (unresolved_infall(i4)) return STEP_HORIZON;
+    }
     // NaN guard on the momenta: every stage value of p^t, p^r, p^phi enters
     // k4, k5, k7 and so the momentum increments, so a non-finite t, r or phi
     // increment (sums of those stage values) implies a non-finite momentum
