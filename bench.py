@@ -68,6 +68,12 @@ SCHW = [1.0, 1.001, 1000.0]
 RESERVE = 2
 BISECT_RAYS = 16384  # speculative width of a bisection round (geon_set_bisect_rays_per_round)
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
+# The mixed path's closed-form right-hand sides (metric_analytic.cuh) for the
+# config-3 metrics, counted by hand (a fused multiply-add counts 2): Alcubierre
+# rhs_stage 60 flops besides one division, one square root and two tanh;
+# Morris-Thorne rhs_planar (the orbit-plane step) 7 besides one division; plus
+# the 104 combine flops of the reference's RK4 step.
+MIXED_CLOSED_FORM_FLOPS_PER_STEP = {"alcubierre": 4 * 60 + 104, "morris_thorne": 4 * 7 + 104}
 CURV_FLOPS_PER_POINT = 20000  # Alcubierre: 9 FD Christoffel evaluations, Riemann, contractions, 16 T(k, k)
 B_C = 3.0 * np.sqrt(3.0)
 # 30M variant: alpha_c = asin(3 sqrt(3) sqrt(1 - 2/30) / 30) = 9.633 deg
@@ -393,7 +399,7 @@ def main():
     if "config1" in legs:
         extras["config1"] = leg("config1", config1_leg, geon, lib, peak64)
     if "config3" in legs:
-        extras["config3"] = leg("config3", config3_leg, geon, lib, 2048, 128, 0)
+        extras["config3"] = leg("config3", config3_leg, geon, lib, 2048, 128, 0, peak32, peak64)
     if "config4" in legs:
         extras["config4"] = leg("config4", config4_leg, geon, 128, peak64)
     if "r30" in legs:
@@ -641,7 +647,20 @@ def config1_leg(geon, lib, peak64):
     return out
 
 
-def config3_leg(geon, lib, n, row_step, check_agreeing=256):
+def fd_fallback_counts():
+    """Algorithmic FP64 work per RK4 step of the finite-difference fallback
+    metrics (Alcubierre, Morris-Thorne), with the operations on structurally
+    zero entries removed, as counted by the generator of the sparse
+    Christoffel symbols (geon_gb300/csrc/gen_sparse_christoffel.py)."""
+    import importlib.util
+    path = os.path.join(ROOT, "geon_gb300", "csrc", "gen_sparse_christoffel.py")
+    spec = importlib.util.spec_from_file_location("gen_sparse_christoffel", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.op_counts()
+
+
+def config3_leg(geon, lib, n, row_step, check_agreeing=256, peak32=None, peak64=None):
     """BASELINE config 3: 2048^2 Alcubierre (R 2, thickness 0.125, v 0.5,
     observer x = -10 looking +x) and Morris-Thorne (b0 1, observer l = 10)
     renders, fov 90, h 0.05, cap 20000: mixed on the full images; FP64 (the
@@ -691,6 +710,29 @@ def config3_leg(geon, lib, n, row_step, check_agreeing=256):
                      "escape_dir_err_rad_max": None if ang is None else float(ang.max()),
                      "cpu_baseline": {"value": float(osteps.sum()) / dt_cpu, "unit": "ray-steps/s", "cores": threads,
                                       "kind": "port", "sample": f"row 0 ({len(yc)} rays, {dt_cpu:.1f} s)"}}
+    counts = fd_fallback_counts()
+    for name in cases:
+        c, o = counts[name], out[name]
+        rays = len(np.arange(0, n, row_step)) * n
+        o["roofline_fp64"] = {
+            "bound": "fp64 pipe", "alg_flops_per_ray_step": c["flops_per_step"],
+            "definition": "the reference's finite-difference fallback (metric/mod.rs:25-69, geodesic.rs:38-59) "
+                          "with operations on structurally zero entries removed: "
+                          f"{c['ops_per_rhs']} per right-hand side from the sparse Christoffel generator, "
+                          f"{c['metric_eval_flops_per_rhs']} for the metric at {c['metric_points_per_rhs']} "
+                          f"distinct points, x4, + {104} RK4 combine; not counted: {c['calls_per_step']} per step",
+            "achieved": o["fp64_ray_steps_per_s"] * c["flops_per_step"] / 1e12, "unit": "TFLOP/s",
+            "sample": f"{rays} rays ({(rays + 127) // 128} blocks of 128 on the GPU), host API wall time"}
+        o["roofline_mixed"] = {
+            "bound": "fp32 pipe", "alg_flops_per_ray_step": MIXED_CLOSED_FORM_FLOPS_PER_STEP[name],
+            "definition": "the mixed path's closed-form right-hand side (metric_analytic.cuh; transcendental "
+                          "and division calls not counted) x4 + 104 RK4 combine",
+            "achieved": o["mixed_ray_steps_per_s"] * MIXED_CLOSED_FORM_FLOPS_PER_STEP[name] / 1e12,
+            "unit": "TFLOP/s"}
+        for key, peak in (("roofline_fp64", peak64), ("roofline_mixed", peak32)):
+            if peak:
+                o[key]["peak"] = peak
+                o[key]["frac"] = o[key]["achieved"] / peak
     out["mixed_ray_steps_per_s_both"] = (sum(out[c]["mixed_total_steps"] for c in cases)
                                          / sum(out[c]["mixed_ms"] / 1e3 for c in cases))
     # both images in ONE persistent launch (geon_render_batch): the rays of the
@@ -918,7 +960,7 @@ def exotic_main(args):
     """BASELINE config 3 as its own line (config3_leg)."""
     import geon_gb300 as geon
     lib = geon._load()
-    out = config3_leg(geon, lib, args.size, args.row_step)
+    out = config3_leg(geon, lib, args.size, args.row_step, 256, ctypes_peak(lib, 0), ctypes_peak(lib, 1))
     _emit(out["workload"], out["mixed_ray_steps_per_s_both"], "ray-steps/s",
           sum(out[c]["mixed_ms"] for c in ("alcubierre", "morris_thorne")), "f32 (mixed)",
           {"config3": out, "timing": "host API wall time"})

@@ -15,6 +15,7 @@ order. Rules (all exact in IEEE arithmetic for finite values):
 Results can differ from the dense code only in the sign of zero entries.
 """
 import os
+import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -278,17 +279,65 @@ MT_EVAL = """  double g22{t}, g33{t};
   mt_g22_g33(M, {x}, &g22{t}, &g33{t});"""
 
 
+ALC_SPEC = [["g00", "g01", "zero", "zero"], ["g01", "one", "zero", "zero"],
+            ["zero", "zero", "one", "zero"], ["zero", "zero", "zero", "one"]]
+MT_SPEC = [["mone", "zero", "zero", "zero"], ["zero", "one", "zero", "zero"],
+           ["zero", "zero", "g22", "zero"], ["zero", "zero", "zero", "g33"]]
+ALC_DEPENDS, MT_DEPENDS = (1, 2, 3), (1, 2)
+
+
+def build_all():
+    alc = build("alcubierre",
+                "Alcubierre (alcubierre.rs:48-63): g depends on x^1..x^3 only; g_tt, g_tx, g_xt vary",
+                ALC_SPEC, ALC_DEPENDS, lambda x, t: ALC_EVAL.format(x=x, t=t))
+    mt = build("morris_thorne",
+               "Morris-Thorne (morris_thorne.rs:22-36): g depends on l and theta; g_thth, g_phph vary",
+               MT_SPEC, MT_DEPENDS, lambda x, t: MT_EVAL.format(x=x, t=t))
+    return alc, mt
+
+
+# Arithmetic of one metric evaluation at one point (alc_g00_g01, mt_g22_g33 in
+# metric_fp64.cuh, which follow alcubierre.rs:33-63 and morris_thorne.rs:22-36),
+# besides the calls counted on their own.
+G_EVAL_FLOPS = {"alcubierre": 17, "morris_thorne": 5}
+G_EVAL_CALLS = {"alcubierre": {"sqrt": 1, "tanh": 2}, "morris_thorne": {"sincos": 1}}
+RK4_COMBINE_FLOPS = 104  # integrator.rs:16-40 on the 8 components: 3 stage points + the weighted sum
+
+
+def op_counts():
+    """Algorithmic FP64 work of one right-hand side and one RK4 step of the
+    finite-difference fallback (metric/mod.rs:25-69, geodesic.rs:38-59) with
+    the operations on structurally zero entries removed: the operations the
+    generator emits (finite differences, inverse, contraction, the sums of the
+    geodesic equation), plus the metric evaluations at the distinct
+    finite-difference points (the centre and +-h along each axis g depends on;
+    along the others the two evaluations are equal bit for bit and their
+    difference is an exact zero)."""
+    out = {}
+    for (text, gen), name, dep in zip(build_all(), ("alcubierre", "morris_thorne"), (ALC_DEPENDS, MT_DEPENDS)):
+        ops = {"mul": 0, "add": 0, "sub": 0, "div": 0}
+        for line in gen.lines:
+            m = re.match(r"\s*const double t\d+ = (.*);$", line)
+            if not m:
+                continue
+            expr = m.group(1)
+            for sym, key in ((" * ", "mul"), (" + ", "add"), (" - ", "sub"), (" / ", "div")):
+                if sym in expr:
+                    ops[key] += 1
+                    break
+        points = 1 + 2 * len(dep)
+        calls = {k: v * points for k, v in G_EVAL_CALLS[name].items()}
+        per_rhs = sum(ops.values()) + points * G_EVAL_FLOPS[name]
+        out[name] = {"ops_per_rhs": ops, "metric_points_per_rhs": points,
+                     "metric_eval_flops_per_rhs": points * G_EVAL_FLOPS[name],
+                     "calls_per_rhs": calls, "flops_per_rhs": per_rhs,
+                     "flops_per_step": 4 * per_rhs + RK4_COMBINE_FLOPS,
+                     "calls_per_step": {k: 4 * v for k, v in calls.items()}}
+    return out
+
+
 def main():
-    alc_spec = [["g00", "g01", "zero", "zero"], ["g01", "one", "zero", "zero"],
-                ["zero", "zero", "one", "zero"], ["zero", "zero", "zero", "one"]]
-    mt_spec = [["mone", "zero", "zero", "zero"], ["zero", "one", "zero", "zero"],
-               ["zero", "zero", "g22", "zero"], ["zero", "zero", "zero", "g33"]]
-    alc, ga = build("alcubierre",
-                    "Alcubierre (alcubierre.rs:48-63): g depends on x^1..x^3 only; g_tt, g_tx, g_xt vary",
-                    alc_spec, (1, 2, 3), lambda x, t: ALC_EVAL.format(x=x, t=t))
-    mt, gm = build("morris_thorne",
-                   "Morris-Thorne (morris_thorne.rs:22-36): g depends on l and theta; g_thth, g_phph vary",
-                   mt_spec, (1, 2), lambda x, t: MT_EVAL.format(x=x, t=t))
+    (alc, ga), (mt, gm) = build_all()
     header = """// GENERATED by gen_sparse_christoffel.py - do not edit by hand.
 //
 // Sparse FP64 Christoffel symbols, bit-identical (up to the sign of zero

@@ -42,7 +42,13 @@ struct AMath<float> {
     return r;
   }
   static __device__ __forceinline__ float div(float a, float b) { return a * rcp(b); }
-  static __device__ __forceinline__ float sqrt(float x) { return __fsqrt_rn(x); }
+  // approximate square root (one MUFU op, relative error below 2^-23; 0 at 0):
+  // the RHS tolerates FP32 error
+  static __device__ __forceinline__ float sqrt(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
   // tanh(x) = sign(x) (1 - 2 / (e^{2|x|} + 1)) with the hardware exponential
   // and reciprocal (two MUFU ops): absolute error ~2e-7, which is what the
   // Alcubierre RHS needs (it uses differences of tanh values near +-1). Large
