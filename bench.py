@@ -785,7 +785,19 @@ def config4_leg(geon, n, peak64, cpu_budget_s=3.0):
     alc = geon.Alcubierre(2.0, 0.125, 0.5, 0.0)
     lo, hi = (-4.0, -4.0, -4.0), (4.0, 4.0, 4.0)
     geon.curvature.grid(alc, lo, hi, (8, 8, 8), nk=16)
-    dt, (pts, ein, nec, _) = _wall(lambda: geon.curvature.grid(alc, lo, hi, (n, n, n), nk=16), 1)
+    dt_fresh, (pts, ein, nec, _) = _wall(lambda: geon.curvature.grid(alc, lo, hi, (n, n, n), nk=16), 1)
+    # the host API as a caller computing grid after grid uses it: the same
+    # caller-owned result arrays each call (fresh arrays add the driver's
+    # first-use setup of 537 MB of host memory, dt_fresh)
+    ein_h, nec_h = np.empty_like(ein), np.empty_like(nec)
+    host_ms = []
+    for _ in range(4):
+        t0 = time.perf_counter()
+        geon.curvature.grid_into(alc, lo, hi, (n, n, n), ein_h, nec_h, nk=16)
+        host_ms.append(1e3 * (time.perf_counter() - t0))
+    dt = float(np.median(host_ms[1:])) / 1e3
+    host_same = bool(np.array_equal(ein_h, ein) and np.array_equal(nec_h, nec))
+    del ein_h, nec_h
     sub = np.arange(0, len(pts), max(1, len(pts) // 1024))
     oein = orc.curvature(2, [2.0, 0.125, 0.5, 0.0], pts[sub], "einstein", math=orc.GEON, nthreads=threads)
     bit_exact = bool(np.array_equal(oein.reshape(-1, 16), ein[sub].reshape(-1, 16)))
@@ -825,7 +837,10 @@ def config4_leg(geon, n, peak64, cpu_budget_s=3.0):
     sch = geon.Schwarzschild(1.0)
     dt_s, rs = _wall(lambda: geon.curvature.ricci_scalar(sch, x), 2)
     return {"workload": f"curvature grid {n}^3 alcubierre (v_s 0.5, R 2, sigma 8) einstein + 16 null T(k,k) per point",
-            "points_per_s": len(pts) / dt, "host_api_ms": 1e3 * dt, "kernel_ms": kernel_ms,
+            "points_per_s": len(pts) / dt, "host_api_ms": 1e3 * dt,
+            "host_api": "geon_curvature_grid into caller-owned host arrays reused across calls: median of 3 after one "
+                        "warm-up, results copied back inside the timed call",
+            "host_api_ms_fresh_arrays": 1e3 * dt_fresh, "host_api_same_bits": host_same, "kernel_ms": kernel_ms,
             "kernel_points_per_s": len(pts) / (1e-3 * kernel_ms),
             "roofline": {"bound": "fp64 pipe", "achieved": ach, "peak": peak64, "unit": "TFLOP/s",
                          "frac": ach / peak64 if peak64 else None, "kernel": "curvature_grid_kernel<Alcubierre>",

@@ -58,24 +58,42 @@ def wec_contraction(metric, x, u):
     return nec_contraction(metric, x, u)
 
 
-def grid(metric, lo, hi, n, t=0.0, nk=16, seed=0x5EED, with_einstein=True, with_k=False):
-    """Einstein tensor and T(k, k) for nk seeded null vectors per point over a
-    regular grid (endpoints included). Returns (points (N, 4), einstein
-    (N, 4, 4) or None, nec (N, nk), k (N, nk, 4) or None)."""
+def _grid_desc(lo, hi, n, t):
     g = _ffi.GeonGrid()
     for i in range(3):
         g.lo[i] = float(lo[i])
         g.hi[i] = float(hi[i])
         g.n[i] = int(n[i])
     g.t = float(t)
+    return g
+
+
+def grid_into(metric, lo, hi, n, einstein, nec, k=None, t=0.0, nk=16, seed=0x5EED):
+    """grid() into caller-owned host arrays (C-contiguous float64): einstein
+    (N, 4, 4) or None, nec (N, nk) (None when nk is 0), k (N, nk, 4) or None.
+    A caller that computes many grids reuses its arrays: host memory that a
+    device copy has not written before costs the driver a first-use setup
+    (about 40 ms for 512 MiB on GB300), a reused array only the copy."""
+    npts = int(n[0]) * int(n[1]) * int(n[2])
+    for a, shape in ((einstein, (npts, 4, 4)), (nec, (npts, nk)), (k, (npts, nk, 4))):
+        if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous or a.size != int(np.prod(shape))):
+            raise ValueError(f"output array must be C-contiguous float64 with {int(np.prod(shape))} elements")
+    check(_ffi.load().geon_curvature_grid(metric.handle, _grid_desc(lo, hi, n, t), int(nk),
+                                          int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                          dp(einstein) if einstein is not None else None,
+                                          dp(nec) if nec is not None else None,
+                                          dp(k) if k is not None else None))
+
+
+def grid(metric, lo, hi, n, t=0.0, nk=16, seed=0x5EED, with_einstein=True, with_k=False):
+    """Einstein tensor and T(k, k) for nk seeded null vectors per point over a
+    regular grid (endpoints included). Returns (points (N, 4), einstein
+    (N, 4, 4) or None, nec (N, nk), k (N, nk, 4) or None)."""
     npts = int(n[0]) * int(n[1]) * int(n[2])
     ein = np.empty((npts, 4, 4)) if with_einstein else None
     nec = np.empty((npts, nk)) if nk else None
     kk = np.empty((npts, nk, 4)) if (with_k and nk) else None
-    check(_ffi.load().geon_curvature_grid(metric.handle, g, int(nk), int(seed) & 0xFFFFFFFFFFFFFFFF,
-                                          dp(ein) if ein is not None else None,
-                                          dp(nec) if nec is not None else None,
-                                          dp(kk) if kk is not None else None))
+    grid_into(metric, lo, hi, n, ein, nec, kk, t=t, nk=nk, seed=seed)
     return grid_points(lo, hi, n, t), ein, nec, kk
 
 
@@ -84,12 +102,7 @@ def grid_dev(metric, lo, hi, n, einstein, nec, nk=16, seed=0x5EED, k_out=None, t
     (N*nk doubles) and k_out (N*nk*4 doubles, or None) are device addresses
     (ints, or objects with data_ptr()); the launch is queued on stream and not
     waited for."""
-    g = _ffi.GeonGrid()
-    for i in range(3):
-        g.lo[i] = float(lo[i])
-        g.hi[i] = float(hi[i])
-        g.n[i] = int(n[i])
-    g.t = float(t)
+    g = _grid_desc(lo, hi, n, t)
 
     def ptr(a):
         if a is None:

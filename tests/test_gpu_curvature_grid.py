@@ -25,6 +25,26 @@ def test_grid_matches_oracle_alcubierre(geon, orc):
     assert not np.array_equal(nec, nec3)
 
 
+def test_grid_into_reused_arrays(geon):
+    """grid_into fills caller-owned arrays (reused across calls) with grid()'s
+    bits, and refuses arrays of the wrong size or layout."""
+    m = geon.Alcubierre(2.0, 0.125, 0.5, 0.0)
+    lo, hi, n = (-4.0, -4.0, -4.0), (4.0, 4.0, 4.0), (6, 5, 4)
+    _, ein, nec, k = geon.curvature.grid(m, lo, hi, n, nk=3, seed=5, with_k=True)
+    e2, n2, k2 = np.full_like(ein, np.nan), np.full_like(nec, np.nan), np.full_like(k, np.nan)
+    for _ in range(2):
+        geon.curvature.grid_into(m, lo, hi, n, e2, n2, k2, nk=3, seed=5)
+        assert np.array_equal(e2, ein) and np.array_equal(n2, nec) and np.array_equal(k2, k)
+    geon.curvature.grid_into(m, lo, hi, n, None, n2, nk=3, seed=5)
+    assert np.array_equal(n2, nec)
+    with pytest.raises(ValueError):
+        geon.curvature.grid_into(m, lo, hi, n, e2[:-1], n2, nk=3)
+    with pytest.raises(ValueError):
+        geon.curvature.grid_into(m, lo, hi, n, e2, np.asfortranarray(n2.reshape(-1, 3)[:, ::-1]), nk=3)
+    with pytest.raises(ValueError):
+        geon.curvature.grid_into(m, lo, hi, n, e2.astype(np.float32), n2, nk=3)
+
+
 def test_grid_morris_thorne_throat_energy_density(geon):
     """Config 4b: b0 = 1, 4096 points over l in [-5, 5]; T_tt at the throat vs -1/(8 pi)."""
     m = geon.MorrisThorne(1.0)
