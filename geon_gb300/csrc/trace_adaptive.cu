@@ -131,6 +131,7 @@ struct AdaptiveStepper {
     return STEP_NONFINITE;
   }
   __device__ __forceinline__ void group_end(const TraceLaunch&) {}
+  __device__ __forceinline__ void check_null(const TraceLaunch&, const double*) {}
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
   }

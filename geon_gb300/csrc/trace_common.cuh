@@ -200,6 +200,7 @@ __device__ __forceinline__ void trace_loop(const TraceLaunch& L) {
             double y0[8];
             load_ray<SRC>(L, ray, y0);
             st.load(L, y0);
+            if constexpr (SRC == SRC_ARRAY) st.check_null(L, y0);  // camera and equatorial rays are null
           }
         }
       }
@@ -288,6 +289,7 @@ __device__ __forceinline__ void trace_loop_multi(const TraceLaunch* __restrict__
             load_ray<SRC>(L, ray, y0);
             st.bind(L, SRC);
             st.load(L, y0);
+            if constexpr (SRC == SRC_ARRAY) st.check_null(L, y0);
           }
         }
       }

@@ -40,6 +40,7 @@ struct Fp64Stepper {
     return STEP_OK;
   }
   __device__ __forceinline__ void group_end(const TraceLaunch&) {}
+  __device__ __forceinline__ void check_null(const TraceLaunch&, const double*) {}
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
   }
@@ -105,6 +106,7 @@ struct Fp64StepperAny {
     return STEP_OK;
   }
   __device__ __forceinline__ void group_end(const TraceLaunch&) {}
+  __device__ __forceinline__ void check_null(const TraceLaunch&, const double*) {}
   __device__ __forceinline__ void finish(const TraceLaunch& L) {
     if (singular) atomicOr(L.flags, 1);
   }

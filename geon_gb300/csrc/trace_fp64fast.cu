@@ -201,6 +201,7 @@ struct FastSchwStepper {
     return STEP_OK;
   }
   __device__ __forceinline__ void group_end(const TraceLaunch&) {}
+  __device__ __forceinline__ void check_null(const TraceLaunch&, const double*) {}
   __device__ __forceinline__ void finish(const TraceLaunch&) {}
 };
 

@@ -135,6 +135,7 @@ struct MixedCore {
   bool planar = (FEAT & FEAT_PLANAR) != 0;
   bool orbit = (FEAT & FEAT_ORBIT) != 0;
   bool decide = (FEAT & FEAT_DECIDE) != 0;
+  bool nullray = true;  // the loaded state is null: the null re-projections apply
   float cap_steps;  // the step cap (max_steps), for the early decision's budget test
   float oe1[3], oe2[3];  // orbit-plane frame (FEAT_ORBIT, FEAT_ORBIT_DYN)
   // rays of metric kind K can step in their orbit-plane frame
@@ -250,9 +251,32 @@ struct MixedCore {
   // and refills come every 16 steps, so this is the same step of every lane of
   // the warp, and every 16th step of each ray): the compensated null
   // re-projection of a ray stepping on its plane.
+  // A ray of an input array is null if g(p, p) at its initial state (FP64,
+  // the metric functor of the FP64 path) cancels to 1e-8 of its largest
+  // term; camera and equatorial rays are null by construction. The null
+  // re-projections hold g(p, p) at 0, so they apply to null rays only: a
+  // timelike or spacelike geodesic keeps the invariant the integration gives
+  // it, as in the reference.
+  template <int K>
+  __device__ __forceinline__ void check_null_k(const TraceLaunch& L, const double y0[8]) {
+    double g[16];
+    metric_g<K>(L.M, y0, g);
+    double sum = 0.0, mag = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const double t = g[4 * i + j] * y0[4 + i] * y0[4 + j];
+        sum += t;
+        mag += fabs(t);
+      }
+    }
+    nullray = fabs(sum) <= 1e-8 * mag;  // false for a non-finite state
+  }
+
   template <int K>
   __device__ __forceinline__ void group_end_k(const TraceLaunch& L) {
-    if (!(L.mixed_flags & MIXED_NULLFIX)) return;
+    if (!(L.mixed_flags & MIXED_NULLFIX) || !nullray) return;
     const bool on_plane = (any_orbit<K>() && orbit) ||
                           (K == KIND_SCHWARZSCHILD && (FEAT & (FEAT_PLANAR | FEAT_PLANAR_DYN)) != 0 &&
                            ((FEAT & FEAT_PLANAR) != 0 || planar));
@@ -385,7 +409,7 @@ struct MixedCore {
 #pragma unroll
     for (int i = 4; i < 8; ++i) two_sum_update(hi[i], lo[i], inc[i]);
     count_step();
-    if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT)) {
+    if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT) && nullray) {
       float s = 0.0f;
       if (K == KIND_SCHWARZSCHILD || K == KIND_MORRIS_THORNE) s = sinf(hi[2]);
       const float x[4] = {hi[0], hi[1], hi[2], hi[3]};
@@ -434,18 +458,21 @@ struct MixedCore {
     const float i0 = sixth * (a0 + k0), i1 = sixth * (a1 + k1), i3 = sixth * (a3 + k3);
     const float i4 = sixth * (a4 + k4), i5 = sixth * (a5 + k5), i7 = sixth * (a7 + k7);
     // The horizon rules (a stage at or inside 2M; an unresolved infall, which
-    // needs r < 3M) are tested only when a stage or the ray is within 3M (or a
-    // stage radius is not a number): one test per step far from the hole.
-    if (K == KIND_SCHWARZSCHILD && (!(rmin > r_near) || hi[1] < r_near)) {
-      if (!(rmin > C.two_m)) return STEP_HORIZON;
-      if (unresolved_infall(i4)) return STEP_HORIZON;
+    // needs r < 3M) apply only when a stage or the ray is within 3M (or a
+    // stage radius is not a number), and the NaN guard on the momenta only
+    // when an increment is not finite: one branch per step covers all three,
+    // tested in their order inside it. (Every stage value of p^t, p^r, p^phi
+    // enters k4, k5, k7 and so the momentum increments, so a non-finite t, r
+    // or phi increment, a sum of those stage values, implies a non-finite
+    // momentum increment; positions that nothing reads, t and phi for the
+    // shadow sink, are then left out by the compiler.)
+    const bool finite = isfinite(i4) && isfinite(i5) && isfinite(i7);
+    const bool near = K == KIND_SCHWARZSCHILD && (!(rmin > r_near) || hi[1] < r_near);
+    if (near || !finite) {
+      if (K == KIND_SCHWARZSCHILD && !(rmin > C.two_m)) return STEP_HORIZON;
+      if (K == KIND_SCHWARZSCHILD && near && unresolved_infall(i4)) return STEP_HORIZON;
+      if (!finite) return STEP_NONFINITE;
     }
-    // NaN guard on the momenta: every stage value of p^t, p^r, p^phi enters
-    // k4, k5, k7 and so the momentum increments, so a non-finite t, r or phi
-    // increment (sums of those stage values) implies a non-finite momentum
-    // increment. Positions that nothing reads (t and phi for the shadow sink)
-    // are then left out by the compiler.
-    if (!(isfinite(i4) && isfinite(i5) && isfinite(i7))) return STEP_NONFINITE;
     fast_two_sum_update(hi[0], lo[0], i0);
     fast_two_sum_update(hi[1], lo[1], i1);
     fast_two_sum_update(hi[3], lo[3], i3);
@@ -458,7 +485,7 @@ struct MixedCore {
     two_sum_update(hi[5], lo[5], i5);
     fast_two_sum_update(hi[7], lo[7], i7);
     count_step();
-    if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT)) {
+    if ((FEAT & FEAT_REPROJECT) && (L.mixed_flags & MIXED_REPROJECT) && nullray) {
       const float x[4] = {hi[0], hi[1], hi[2], hi[3]};
       const float p[4] = {hi[4], hi[5], 0.0f, hi[7]};
       const float pt = null_pt<K, float>(C, x, p, 1.0f, hi[4]);
@@ -558,6 +585,9 @@ struct MixedStepper : MixedCore<FEAT> {
   __device__ __forceinline__ int terminate(const TraceLaunch& L) const { return this->template terminate_k<K>(L); }
   __device__ __forceinline__ int step(const TraceLaunch& L) { return this->template step_k<K>(L); }
   __device__ __forceinline__ void group_end(const TraceLaunch& L) { this->template group_end_k<K>(L); }
+  __device__ __forceinline__ void check_null(const TraceLaunch& L, const double y0[8]) {
+    this->template check_null_k<K>(L, y0);
+  }
 };
 
 // The stepper of a launch whose rays have different metric kinds (several
@@ -611,6 +641,14 @@ struct MixedStepperAny : MixedCore<FEAT> {
       case KIND_SCHWARZSCHILD: this->template group_end_k<KIND_SCHWARZSCHILD>(L); return;
       case KIND_MORRIS_THORNE: this->template group_end_k<KIND_MORRIS_THORNE>(L); return;
       default: return;
+    }
+  }
+  __device__ __forceinline__ void check_null(const TraceLaunch& L, const double y0[8]) {
+    switch (kind) {
+      case KIND_SCHWARZSCHILD: this->template check_null_k<KIND_SCHWARZSCHILD>(L, y0); return;
+      case KIND_MORRIS_THORNE: this->template check_null_k<KIND_MORRIS_THORNE>(L, y0); return;
+      case KIND_ALCUBIERRE: this->template check_null_k<KIND_ALCUBIERRE>(L, y0); return;
+      default: this->template check_null_k<KIND_MINKOWSKI>(L, y0); return;
     }
   }
 };

@@ -242,12 +242,16 @@ void geon_set_mixed_reproject(int on);
  * in the chart whatever this says). No counterpart in the reference. */
 void geon_set_mixed_orbit_plane(int on);
 int geon_get_mixed_orbit_plane(void);
-/* Compensated null re-projection for GEON_MIXED rays on their plane (shadow
- * rays; Schwarzschild and Morris-Thorne rays in their orbit-plane frame): every
- * 16 steps of a ray, g(p, p) is formed in float-float from the compensated
- * state and one Newton step on g(p, p) = 0 in p^t is added to p^t with its
- * rounding error kept (null drift ~1e-13, the FP64 path's, at ~3 % of the
- * step's cost). Default on (1); served requests always use it. No counterpart
+/* Compensated null re-projection for GEON_MIXED null rays on their plane
+ * (shadow rays; Schwarzschild and Morris-Thorne rays in their orbit-plane
+ * frame): after every 16 steps of a ray, g(p, p) is formed in float-float
+ * from the compensated state and one Newton step on g(p, p) = 0 in p^t is
+ * added to p^t with its rounding error kept (null drift ~1e-13, the FP64
+ * path's, at ~3 % of the step's cost). Camera and equatorial rays are null by
+ * construction; a ray of a geon_trace array is null if g(p, p) at its initial
+ * state cancels to 1e-8 of its largest term (FP64), and a timelike or
+ * spacelike ray keeps the invariant its integration gives it, as in the
+ * reference. Default on (1); served requests always use it. No counterpart
  * in the reference. */
 void geon_set_mixed_null_fix(int on);
 int geon_get_mixed_null_fix(void);

@@ -197,3 +197,50 @@ def test_shadow_dev_api(geon):
     torch.cuda.synchronize()
     ref, _, _, rst = geon.shadow.bisect(m, 20.0, lo.cpu().numpy(), hi.cpu().numpy(), iters=12)
     assert np.array_equal(ac.cpu().numpy(), ref) and np.array_equal(st.cpu().numpy(), rst)
+
+
+def test_mixed_trace_edge_cases(geon):
+    """The reference's loop structure in the mixed path (geodesic.rs:62-117):
+    the termination test before every step, the step cap with steps_taken =
+    max_steps, the NaN guard keeping the pre-step state; the same classes and
+    counts as the FP64 path on rays that end at once or at the cap. One
+    documented difference: a step with a stage at or inside 2M is a horizon
+    step in the mixed path (Captured, the step counted, the state kept), also
+    when the stage radius is -inf; the FP64 path, like the reference, lets
+    that step overflow and its NaN guard reports Diverged."""
+    m = geon.Schwarzschild(1.0, 1.001, 100.0)
+    y = geon.shadow.equatorial_ray(m, 20.0, np.array([0.1, 0.3, 1.2]))
+    cases = np.concatenate([
+        y,
+        [[0.0, 1.5, np.pi / 2, 0.0, 1.0, -1.0, 0.0, 0.0]],     # starts inside the capture radius
+        [[0.0, 150.0, np.pi / 2, 0.0, 1.0, 1.0, 0.0, 0.0]],    # starts beyond escape
+        [[0.0, np.nan, np.pi / 2, 0.0, 1.0, 1.0, 0.0, 0.0]],   # non-finite r: Diverged at once
+        [[0.0, 20.0, np.pi / 2, 0.0, 1.0, -1e300, 0.0, 0.0]],  # p^r overflows FP32: stage radius -inf
+        [[0.0, 20.0, 1.0, 0.3, 1.0, -0.5, 0.01, 0.02]],        # off the equator (orbit-plane frame)
+    ])
+    same = np.arange(len(cases)) != 6
+    for max_steps in [0, 1, 7, 16, 17]:
+        r64 = geon.trace(m, cases, 0.05, max_steps, precision="fp64")
+        rmx = geon.trace(m, cases, 0.05, max_steps, precision="mixed")
+        assert np.array_equal(rmx.termination[same], r64.termination[same]), max_steps
+        assert np.array_equal(rmx.steps_taken[same], r64.steps_taken[same]), max_steps
+        if max_steps == 0:  # no test and no step: every ray Diverged with its loaded state
+            assert np.all(rmx.termination == 0) and np.all(rmx.steps_taken == 0)
+        else:
+            assert rmx.termination[4] == 2 and rmx.final_state[4, 1] == 150.0
+            assert rmx.termination[5] == 0 and np.isnan(rmx.final_state[5, 1])
+            assert rmx.termination[6] == 1 and rmx.steps_taken[6] == 1  # horizon step, state kept
+        assert rmx.final_state[6, 1] == 20.0
+    r64 = geon.trace(m, cases, 0.05, 5000, precision="fp64")
+    rmx = geon.trace(m, cases, 0.05, 5000, precision="mixed")
+    assert np.array_equal(rmx.termination[same], r64.termination[same])
+    esc = r64.termination == 2
+    assert np.abs(rmx.steps_taken[esc] - r64.steps_taken[esc]).max() <= 1
+    # ray 7 is timelike (g(p, p) = -0.47): no null re-projection, its invariant
+    # kept as the FP64 path keeps it
+    assert r64.null_residual[7] > 0.4
+    assert abs(rmx.null_residual[7] - r64.null_residual[7]) <= 1e-6 * r64.null_residual[7]
+    # null rays are re-projected: drift at the FP64 path's level
+    assert np.all(rmx.null_residual[[1, 2]] < 1e-11)
+    empty = geon.trace(m, np.zeros((0, 8)), 0.05, 10, precision="mixed")
+    assert empty.termination.shape == (0,)
