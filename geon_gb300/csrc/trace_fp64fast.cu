@@ -11,11 +11,14 @@
 // geodesic.rs:38-59):
 //   * one reciprocal, of D = r (r - 2M) sin(theta), in place of the reference's
 //     five divisions: 1/r, 1/(r - 2M) and cot(theta) are products with 1/D;
-//   * sin and cos of the polar angle once per step (dm::sincos_det); the three
+//   * sin and cos of the polar angle carried from step to step: the three
 //     later stages move theta by d = c h k^theta and take sin, cos of
 //     theta0 + d by the angle-addition formula with Taylor polynomials of sin d
 //     and cos d (|d| <= 1/32, truncation below 1e-19; larger offsets evaluate
-//     sincos_det of the stage angle itself);
+//     sincos_det of the stage angle itself), the next step's theta0 the same
+//     way from the step's own increment, and sincos_det afresh every 16 steps
+//     of a ray (at load and after each group of 16 steps), so the carried
+//     values stay within a few ulp;
 //   * the sparse sums with fused multiply-adds, the Christoffel symbols shared
 //     between their symmetric entries, and no stage positions for t and phi
 //     (nothing reads them);
@@ -101,10 +104,17 @@ template <bool PLANAR>
 struct FastSchwStepper {
   double y[8];
   bool on_plane = PLANAR;
+  // sin and cos of y[2] for the general step, carried from step to step by
+  // the angle-addition formula and taken afresh every 16 steps of the ray (at
+  // load and after each group of 16 steps)
+  double sth = 0.0, cth = 1.0;
   __device__ __forceinline__ void load(const TraceLaunch&, const double y0[8]) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) y[i] = y0[i];
-    if (!PLANAR) on_plane = y[2] == 1.5707963267948966 && y[6] == 0.0;
+    if (!PLANAR) {
+      on_plane = y[2] == 1.5707963267948966 && y[6] == 0.0;
+      if (!on_plane) dm::sincos_det(y[2], &sth, &cth);
+    }
   }
   __device__ __forceinline__ void to_double(double out[8]) const {
 #pragma unroll
@@ -151,8 +161,7 @@ struct FastSchwStepper {
       y[0] = n0; y[1] = n1; y[3] = n3; y[4] = n4; y[5] = n5; y[7] = n7;
       return STEP_OK;
     }
-    double s0, c0;
-    dm::sincos_det(y[2], &s0, &c0);
+    const double s0 = sth, c0 = cth;
     double k4, k5, k6, k7;
     double p0 = y[4], p1 = y[5], p2 = y[6], p3 = y[7];
     fast::rhs(m, two_m, y[1], s0, c0, p0, p1, p2, p3, &k4, &k5, &k6, &k7);
@@ -196,11 +205,24 @@ struct FastSchwStepper {
       finite &= isfinite(yn[i]);
     }
     if (!finite) return STEP_NONFINITE;
+    // sin and cos at the new theta from those at the old one (the difference of
+    // two nearby doubles is exact)
+    const double dth = yn[2] - y[2];
+    if (fabs(dth) <= 0.03125) {
+      double sn, cn;
+      fast::sincos_offset(s0, c0, dth, &sn, &cn);
+      sth = sn;
+      cth = cn;
+    } else {
+      dm::sincos_det(yn[2], &sth, &cth);
+    }
 #pragma unroll
     for (int i = 0; i < 8; ++i) y[i] = yn[i];
     return STEP_OK;
   }
-  __device__ __forceinline__ void group_end(const TraceLaunch&) {}
+  __device__ __forceinline__ void group_end(const TraceLaunch&) {
+    if (!PLANAR && !on_plane) dm::sincos_det(y[2], &sth, &cth);
+  }
   __device__ __forceinline__ void check_null(const TraceLaunch&, const double*) {}
   __device__ __forceinline__ void finish(const TraceLaunch&) {}
 };

@@ -240,7 +240,8 @@ def test_mixed_trace_edge_cases(geon):
     # kept as the FP64 path keeps it
     assert r64.null_residual[7] > 0.4
     assert abs(rmx.null_residual[7] - r64.null_residual[7]) <= 1e-6 * r64.null_residual[7]
-    # null rays are re-projected: drift at the FP64 path's level
-    assert np.all(rmx.null_residual[[1, 2]] < 1e-11)
+    # null rays are re-projected (every 16 steps; at h = 0.05 the drift of the
+    # steps since the last one stays below 1e-10)
+    assert np.all(rmx.null_residual[[1, 2]] < 1e-10)
     empty = geon.trace(m, np.zeros((0, 8)), 0.05, 10, precision="mixed")
     assert empty.termination.shape == (0,)
