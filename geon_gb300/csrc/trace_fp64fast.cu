@@ -10,7 +10,8 @@
 // cheaper, per right-hand side (schwarzschild.rs:61-107 fused with
 // geodesic.rs:38-59):
 //   * one reciprocal, of D = r (r - 2M) sin(theta), in place of the reference's
-//     five divisions: 1/r, 1/(r - 2M) and cot(theta) are products with 1/D;
+//     five divisions: 1/r, Gamma^t_tr = M / (r (r - 2M)) and cot(theta) are
+//     products with 1/D, and Gamma^r_tt = Gamma^t_tr f^2 with f = 1 - 2M/r;
 //   * sin and cos of the polar angle carried from step to step: the three
 //     later stages move theta by d = c h k^theta and take sin, cos of
 //     theta0 + d by the angle-addition formula with Taylor polynomials of sin d
@@ -67,13 +68,14 @@ __device__ __forceinline__ void rhs(double m, double two_m, double r, double s, 
   const double se = pole ? 1.0 : s;
   const double rrm = r * rm;
   const double iD = __drcp_rn(rrm * se);
-  const double ir = (rm * iD) * se;    // 1 / r
-  const double irm = (r * iD) * se;    // 1 / (r - 2M)
+  const double iDs = iD * se;          // 1 / (r (r - 2M))
+  const double ir = rm * iDs;          // 1 / r
   const double cot = pole ? 0.0 : c * (rrm * iD);
-  const double u = (m * ir) * irm;     // Gamma^t_tr = M / (r^2 f) = -Gamma^r_rr
-  const double grtt = (m * ir) * (rm * (ir * ir));  // Gamma^r_tt = M f / r^2
+  const double u = m * iDs;            // Gamma^t_tr = M / (r^2 f) = -Gamma^r_rr
+  const double f = rm * ir;            // 1 - 2M/r
+  const double grtt = u * (f * f);     // Gamma^r_tt = M f / r^2 = Gamma^t_tr f^2
   const double q = fma(s * s, p3 * p3, p2 * p2);    // p_theta^2 + sin^2 p_phi^2
-  *k4 = (-2.0 * u * p0) * p1;
+  *k4 = ((-two_m * iDs) * p0) * p1;    // -2 Gamma^t_tr p^t p^r
   *k5 = fma(rm, q, fma(u, p1 * p1, -(grtt * p0) * p0));
   *k6 = fma(s * c, p3 * p3, (-2.0 * ir * p1) * p2);
   *k7 = (-2.0 * p3) * fma(ir, p1, cot * p2);
@@ -85,10 +87,10 @@ __device__ __forceinline__ void rhs_planar(double m, double two_m, double r, dou
   const double rm = r - two_m;
   const double iD = __drcp_rn(r * rm);
   const double ir = rm * iD;
-  const double irm = r * iD;
-  const double u = (m * ir) * irm;
-  const double grtt = (m * ir) * (rm * (ir * ir));
-  *k4 = (-2.0 * u * p0) * p1;
+  const double u = m * iD;
+  const double f = rm * ir;
+  const double grtt = u * (f * f);
+  *k4 = ((-two_m * iD) * p0) * p1;
   *k5 = fma(rm, p3 * p3, fma(u, p1 * p1, -(grtt * p0) * p0));
   *k7 = (-2.0 * p3) * (ir * p1);
 }
