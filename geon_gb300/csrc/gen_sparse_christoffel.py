@@ -336,8 +336,9 @@ def op_counts():
     return out
 
 
-def main():
-    (alc, ga), (mt, gm) = build_all()
+def header_text():
+    """The text of christoffel_sparse.cuh."""
+    (alc, _), (mt, _) = build_all()
     header = """// GENERATED by gen_sparse_christoffel.py - do not edit by hand.
 //
 // Sparse FP64 Christoffel symbols, bit-identical (up to the sign of zero
@@ -347,10 +348,14 @@ def main():
 // everything else is evaluated in the dense algorithm's order.
 #pragma once
 """
-    text = header + "\n" + alc + "\n\n" + mt + "\n"
+    return header + "\n" + alc + "\n\n" + mt + "\n"
+
+
+def main():
     with open(os.path.join(HERE, "christoffel_sparse.cuh"), "w") as f:
-        f.write(text)
-    print(f"alcubierre: {ga.n} temporaries; morris-thorne: {gm.n} temporaries")
+        f.write(header_text())
+    for name, c in op_counts().items():
+        print(f"{name}: {c['ops_per_rhs']} per right-hand side, {c['flops_per_step']} flops per RK4 step")
 
 
 if __name__ == "__main__":
