@@ -813,6 +813,7 @@ int geon_render_batch(const geon_render_item* items, size_t n) {
     }
     jobs[j] = L;
     D.start[j + 1] = D.start[j] + nsamp;
+    D.kind_mask |= 1 << L.M.kind;
   }
   D.queue = wsu;
   GEON_CUDA(djobs.alloc(sizeof(TraceLaunch) * n, s));

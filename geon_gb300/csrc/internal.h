@@ -134,6 +134,7 @@ cudaError_t launch_trace_adaptive(const TraceLaunch& L, int src, int sink, cudaS
 constexpr int MULTI_MAX_JOBS = 8;
 struct MultiDesc {
   int njobs;
+  int kind_mask;  // bit K set when a job of the launch has metric kind K (the mixed kernel's variant)
   int64_t start[MULTI_MAX_JOBS + 1];
   unsigned long long* queue;
 };

@@ -15,6 +15,8 @@
 // fused multiply-add in the FP32 code is written out explicitly.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "internal.h"
 #include "metric_analytic.cuh"
 #include "orbit_frame.cuh"
@@ -593,10 +595,31 @@ struct MixedStepper : MixedCore<FEAT> {
 // The stepper of a launch whose rays have different metric kinds (several
 // renders traced by one persistent kernel): each lane keeps the kind of the
 // ray it holds and branches on it; lanes of a warp mostly hold rays of one job,
-// claimed together, so the branch is mostly uniform.
-template <int FEAT>
+// claimed together, so the branch is mostly uniform. KMASK (bit K for metric
+// kind K) lists the kinds the launch holds: only their steps are compiled in,
+// which keeps the kernel's registers near those of the largest single step.
+template <int FEAT, int KMASK = 15>
 struct MixedStepperAny : MixedCore<FEAT> {
   int kind = KIND_MINKOWSKI;
+  // f(std::integral_constant<int, K>) for the lane's kind K among KMASK's
+  template <class F>
+  __device__ __forceinline__ auto on_kind(F&& f) const {
+    using S = std::integral_constant<int, KIND_SCHWARZSCHILD>;
+    using T = std::integral_constant<int, KIND_MORRIS_THORNE>;
+    using A = std::integral_constant<int, KIND_ALCUBIERRE>;
+    using M = std::integral_constant<int, KIND_MINKOWSKI>;
+    if constexpr ((KMASK >> KIND_SCHWARZSCHILD) & 1) {
+      if (kind == KIND_SCHWARZSCHILD || KMASK == (1 << KIND_SCHWARZSCHILD)) return f(S{});
+    }
+    if constexpr ((KMASK >> KIND_MORRIS_THORNE) & 1) {
+      if (kind == KIND_MORRIS_THORNE || (KMASK & ~((1 << KIND_SCHWARZSCHILD) | (1 << KIND_MORRIS_THORNE))) == 0)
+        return f(T{});
+    }
+    if constexpr ((KMASK >> KIND_ALCUBIERRE) & 1) {
+      if (kind == KIND_ALCUBIERRE || (KMASK >> KIND_MINKOWSKI & 1) == 0) return f(A{});
+    }
+    return f(M{});
+  }
   // A lane takes a ray of job L: its metric constants and kind.
   __device__ __forceinline__ void bind(const TraceLaunch& L, int src) {
     this->setup(L);
@@ -605,51 +628,22 @@ struct MixedStepperAny : MixedCore<FEAT> {
                   (kind == KIND_SCHWARZSCHILD || kind == KIND_MORRIS_THORNE);
   }
   __device__ __forceinline__ void load(const TraceLaunch& L, const double y0[8]) {
-    switch (kind) {
-      case KIND_SCHWARZSCHILD: this->template load_k<KIND_SCHWARZSCHILD>(L, y0); return;
-      case KIND_MORRIS_THORNE: this->template load_k<KIND_MORRIS_THORNE>(L, y0); return;
-      case KIND_ALCUBIERRE: this->template load_k<KIND_ALCUBIERRE>(L, y0); return;
-      default: this->template load_k<KIND_MINKOWSKI>(L, y0); return;
-    }
+    on_kind([&](auto k) { this->template load_k<decltype(k)::value>(L, y0); });
   }
   __device__ __forceinline__ void to_double(double out[8]) const {
-    switch (kind) {
-      case KIND_SCHWARZSCHILD: this->template to_double_k<KIND_SCHWARZSCHILD>(out); return;
-      case KIND_MORRIS_THORNE: this->template to_double_k<KIND_MORRIS_THORNE>(out); return;
-      case KIND_ALCUBIERRE: this->template to_double_k<KIND_ALCUBIERRE>(out); return;
-      default: this->template to_double_k<KIND_MINKOWSKI>(out); return;
-    }
+    on_kind([&](auto k) { this->template to_double_k<decltype(k)::value>(out); });
   }
   __device__ __forceinline__ int terminate(const TraceLaunch& L) const {
-    switch (kind) {
-      case KIND_SCHWARZSCHILD: return this->template terminate_k<KIND_SCHWARZSCHILD>(L);
-      case KIND_MORRIS_THORNE: return this->template terminate_k<KIND_MORRIS_THORNE>(L);
-      case KIND_ALCUBIERRE: return this->template terminate_k<KIND_ALCUBIERRE>(L);
-      default: return this->template terminate_k<KIND_MINKOWSKI>(L);
-    }
+    return on_kind([&](auto k) { return this->template terminate_k<decltype(k)::value>(L); });
   }
   __device__ __forceinline__ int step(const TraceLaunch& L) {
-    switch (kind) {
-      case KIND_SCHWARZSCHILD: return this->template step_k<KIND_SCHWARZSCHILD>(L);
-      case KIND_MORRIS_THORNE: return this->template step_k<KIND_MORRIS_THORNE>(L);
-      case KIND_ALCUBIERRE: return this->template step_k<KIND_ALCUBIERRE>(L);
-      default: return this->template step_k<KIND_MINKOWSKI>(L);
-    }
+    return on_kind([&](auto k) { return this->template step_k<decltype(k)::value>(L); });
   }
   __device__ __forceinline__ void group_end(const TraceLaunch& L) {
-    switch (kind) {
-      case KIND_SCHWARZSCHILD: this->template group_end_k<KIND_SCHWARZSCHILD>(L); return;
-      case KIND_MORRIS_THORNE: this->template group_end_k<KIND_MORRIS_THORNE>(L); return;
-      default: return;
-    }
+    on_kind([&](auto k) { this->template group_end_k<decltype(k)::value>(L); });
   }
   __device__ __forceinline__ void check_null(const TraceLaunch& L, const double y0[8]) {
-    switch (kind) {
-      case KIND_SCHWARZSCHILD: this->template check_null_k<KIND_SCHWARZSCHILD>(L, y0); return;
-      case KIND_MORRIS_THORNE: this->template check_null_k<KIND_MORRIS_THORNE>(L, y0); return;
-      case KIND_ALCUBIERRE: this->template check_null_k<KIND_ALCUBIERRE>(L, y0); return;
-      default: this->template check_null_k<KIND_MINKOWSKI>(L, y0); return;
-    }
+    on_kind([&](auto k) { this->template check_null_k<decltype(k)::value>(L, y0); });
   }
 };
 
@@ -736,17 +730,19 @@ static cudaError_t launch_mst(const TraceLaunch& L, cudaStream_t s) {
 // single-render kernels, so each image equals its single render). The rays'
 // states are prepared and shaded per render by the three-kernel render's
 // prepare and shade kernels.
+template <int KMASK>
 __global__ void __launch_bounds__(TRACE_BLOCK) trace_multi_mixed_kernel(const TraceLaunch* jobs, const MultiDesc D) {
-  trace_loop_multi<MixedStepperAny<FEAT_ORBIT_DYN>, SRC_STATE, SINK_STATE>(jobs, D);
+  trace_loop_multi<MixedStepperAny<FEAT_ORBIT_DYN, KMASK>, SRC_STATE, SINK_STATE>(jobs, D);
 }
 
-cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s) {
+template <int KMASK>
+static cudaError_t launch_multi_mixed_k(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s) {
   static int sms = 0, per_sm = 0;
   if (sms == 0) {
     int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_multi_mixed_kernel, TRACE_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_multi_mixed_kernel<KMASK>, TRACE_BLOCK, 0);
     per_sm = occ < 1 ? 1 : occ;
   }
   const int64_t n = D.start[D.njobs];
@@ -754,8 +750,23 @@ cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D
   const int64_t slots = persistent_slots(sms, per_sm, reserve);
   const int64_t need = (n + TRACE_BLOCK - 1) / TRACE_BLOCK;
   const int grid = (int)(need < slots ? need : slots);
-  trace_multi_mixed_kernel<<<grid < 1 ? 1 : grid, TRACE_BLOCK, 0, s>>>(jobs, D);
+  trace_multi_mixed_kernel<KMASK><<<grid < 1 ? 1 : grid, TRACE_BLOCK, 0, s>>>(jobs, D);
   return cudaGetLastError();
+}
+
+// One kernel per set of metric kinds a batch can hold that is worth its own
+// code: one kind, Alcubierre with Morris-Thorne (the exotic pair), and any.
+cudaError_t launch_trace_multi_mixed(const TraceLaunch* jobs, const MultiDesc& D, float reserve, cudaStream_t s) {
+  constexpr int S = 1 << KIND_SCHWARZSCHILD, T = 1 << KIND_MORRIS_THORNE, A = 1 << KIND_ALCUBIERRE,
+                M = 1 << KIND_MINKOWSKI;
+  switch (D.kind_mask) {
+    case S: return launch_multi_mixed_k<S>(jobs, D, reserve, s);
+    case T: return launch_multi_mixed_k<T>(jobs, D, reserve, s);
+    case A: return launch_multi_mixed_k<A>(jobs, D, reserve, s);
+    case M: return launch_multi_mixed_k<M>(jobs, D, reserve, s);
+    case A | T: return launch_multi_mixed_k<A | T>(jobs, D, reserve, s);
+    default: return launch_multi_mixed_k<S | T | A | M>(jobs, D, reserve, s);
+  }
 }
 
 // Serving engine kernel for the mixed-precision classes (serve_common.cuh),
