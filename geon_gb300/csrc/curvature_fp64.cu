@@ -35,6 +35,7 @@ namespace geon {
 
 constexpr int CURV_PPB = 16;       // points per block
 constexpr int CURV_THREADS = 128;
+static_assert(CURV_PPB <= 32 && CURV_THREADS >= 32 + CURV_PPB, "the tetrads run on the second warp");
 
 // Axes g depends on (bit a for x^a).
 template <int K>
@@ -334,8 +335,9 @@ curvature_kernel(const MetricDesc M, int what, const double* __restrict__ xs, in
     }
     double x[4];
     point(pt, x);
-    double gi[16];
-    if (!metric_g_inv<K>(M, x, gi)) atomicOr(flags, 1);
+    double g[16], gi[16];
+    metric_g<K>(M, x, g);
+    if (!metric_g_inv_given<K>(M, x, g, gi)) atomicOr(flags, 1);
     double rs = 0.0;  // curvature.rs:87-97
 #pragma unroll
     for (int q = 0; q < 16; ++q) rs += gi[q] * ric[q];
@@ -343,8 +345,6 @@ curvature_kernel(const MetricDesc M, int what, const double* __restrict__ xs, in
       out[pt] = rs;
       return;
     }
-    double g[16];
-    metric_g<K>(M, x, g);
     const double factor = 1.0 / (8.0 * 3.141592653589793);
     for (int q = 0; q < 16; ++q) {
       const double ein = ric[q] - 0.5 * g[q] * rs;             // curvature.rs:99-110
@@ -359,19 +359,22 @@ curvature_kernel(const MetricDesc M, int what, const double* __restrict__ xs, in
   double* TT = RIC;
   double* TET = G;                                    // [PPB][16]
   int* TOK = (int*)(G + CURV_PPB * 16);               // [PPB]
+  // The Einstein and stress-energy tensors on the first CURV_PPB threads and,
+  // for the grid job, the tetrads on as many threads of the next warp (both
+  // start from g of the point, evaluated on each side), so the block's serial
+  // part is the longer of the two instead of their sum.
   if (tid < CURV_PPB && p0 + tid < n) {
     const int p = tid;
     const int64_t pt = p0 + p;
     double* ric = RIC + 16 * p;
     double x[4];
     point(pt, x);
-    double gi[16];
-    if (!metric_g_inv<K>(M, x, gi)) atomicOr(flags, 1);
+    double g[16], gi[16];
+    metric_g<K>(M, x, g);
+    if (!metric_g_inv_given<K>(M, x, g, gi)) atomicOr(flags, 1);
     double rs = 0.0;  // curvature.rs:87-97
 #pragma unroll
     for (int q = 0; q < 16; ++q) rs += gi[q] * ric[q];
-    double g[16];
-    metric_g<K>(M, x, g);
     const double factor = 1.0 / (8.0 * 3.141592653589793);
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
@@ -379,12 +382,14 @@ curvature_kernel(const MetricDesc M, int what, const double* __restrict__ xs, in
       if (what == 6 && out) out[16 * pt + q] = ein;
       ric[q] = ein * factor;                           // curvature.rs:112-122
     }
-    if (what == 6) {
-      double tet[16];
-      TOK[p] = point_tetrad(g, tet) ? 1 : 0;
+  } else if (what == 6 && tid >= 32 && tid < 32 + CURV_PPB && p0 + (tid - 32) < n) {
+    const int p = tid - 32;
+    double x[4], g[16], tet[16];
+    point(p0 + p, x);
+    metric_g<K>(M, x, g);
+    TOK[p] = point_tetrad(g, tet) ? 1 : 0;
 #pragma unroll
-      for (int q = 0; q < 16; ++q) TET[16 * p + q] = tet[q];
-    }
+    for (int q = 0; q < 16; ++q) TET[16 * p + q] = tet[q];
   }
   __syncthreads();
 

@@ -274,6 +274,15 @@ __device__ __forceinline__ bool metric_g_inv(const MetricDesc& M, const double x
   }
 }
 
+// g^-1 for a point whose g is already at hand: the same values as
+// metric_g_inv (the default inverts g(x), which is g; the overrides ignore it).
+template <int K>
+__device__ __forceinline__ bool metric_g_inv_given(const MetricDesc& M, const double x[4], const double g[16],
+                                                   double gi[16]) {
+  if (K == KIND_MINKOWSKI || K == KIND_SCHWARZSCHILD) return metric_g_inv<K>(M, x, gi);
+  return inv4(g, gi);
+}
+
 // Default dg: central differences with (gp - gm) / two_h (mod.rs:25-43).
 template <int K>
 __device__ __forceinline__ void metric_dg_fd(const MetricDesc& M, const double x[4], double dg[64]) {

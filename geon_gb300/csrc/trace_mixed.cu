@@ -249,10 +249,6 @@ struct MixedCore {
     if constexpr ((FEAT & (FEAT_DECIDE | FEAT_DECIDE_DYN)) != 0) ++nsteps;
   }
 
-  // After every group of 16 steps a ray survives (rays start at a warp refill
-  // and refills come every 16 steps, so this is the same step of every lane of
-  // the warp, and every 16th step of each ray): the compensated null
-  // re-projection of a ray stepping on its plane.
   // A ray of an input array is null if g(p, p) at its initial state (FP64,
   // the metric functor of the FP64 path) cancels to 1e-8 of its largest
   // term; camera and equatorial rays are null by construction. The null
@@ -276,6 +272,10 @@ struct MixedCore {
     nullray = fabs(sum) <= 1e-8 * mag;  // false for a non-finite state
   }
 
+  // After every group of 16 steps a ray survives (rays start at a warp refill
+  // and refills come every 16 steps, so this is the same step of every lane of
+  // the warp, and every 16th step of each ray): the compensated null
+  // re-projection of a null ray stepping on its plane.
   template <int K>
   __device__ __forceinline__ void group_end_k(const TraceLaunch& L) {
     if (!(L.mixed_flags & MIXED_NULLFIX) || !nullray) return;
