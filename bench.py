@@ -831,6 +831,7 @@ def config4_leg(geon, n, peak64, cpu_budget_s=3.0):
     g = mt.g(mpts[i0])
     T = geon.curvature.stress_energy(mt, mpts[i0])
     ttt_mixed = float(np.linalg.inv(g)[0, 0] * T[0, 0])  # T^t_t at the point nearest the throat
+    t_tt = float(T[0, 0])  # T_tt there, the quantity the reference prints against -1/(8 pi)
     rng = np.random.default_rng(7)
     x = np.stack([np.zeros(100000), rng.uniform(3.0, 50.0, 100000), rng.uniform(0.1, np.pi - 0.1, 100000),
                   rng.uniform(0.0, 2 * np.pi, 100000)], axis=1)
@@ -849,7 +850,8 @@ def config4_leg(geon, n, peak64, cpu_budget_s=3.0):
             "device_api_same_bits": dev_same, "bit_exact_vs_oracle_geon_sample": bit_exact,
             "bit_exact_vs_oracle_libm_sample": bit_exact_libm,
             "morris_thorne_line": {"points": 4096, "ms": 1e3 * dt_mt, "points_per_s": 4096 / dt_mt,
-                                   "T_t_t_nearest_throat": ttt_mixed, "l_nearest_throat": float(mpts[i0, 1]),
+                                   "T_tt_nearest_throat": t_tt, "T_t_t_nearest_throat": ttt_mixed,
+                                   "l_nearest_throat": float(mpts[i0, 1]),
                                    "minus_1_over_8pi": -1.0 / (8.0 * np.pi)},
             "schwarzschild_vacuum": {"points": 100000, "ms": 1e3 * dt_s, "points_per_s": 1e5 / dt_s,
                                      "max_abs_ricci_scalar": float(np.max(np.abs(rs))),
