@@ -14,6 +14,9 @@ Inputs are synthetic and seeded.
 
 value = useful ray-steps (sweep steps + the bisections' sequential-path steps)
 per second of device time with inputs resident in HBM (mixed FP32/FP64 path).
+The mixed path runs the bisection rounds first and then the sweep on the whole
+GPU (the rounds take a few ms alone); the FP64 path runs them beside the
+sweep (`--schedule`).
 Beside it, in the same JSON line (rank 0, full workload):
   accuracy      mixed vs FP64 classes on 1/32 of the sweep, traced with the
                 timed planar step, disagreements settled by the FP64 arbiter
@@ -222,9 +225,14 @@ def leg(name, fn, *a, **kw):
 
 
 class SweepRunner:
-    """One step of the headline workload on the GPU: the sweep on stream sa
-    (persistent grid keeping `reserve` block slots per SM free) and the
-    bisections on stream sb, CUDA events on both."""
+    """One step of the headline workload on the GPU: the sweep on stream sa and
+    the bisections on stream sb, CUDA events on both. Two schedules. Serial
+    (the mixed path's default): the bisection rounds first, alone on the GPU
+    (a few ms: each round is as long as its slowest ray takes to settle, and
+    alone every ray runs at full speed), then the sweep on every block slot.
+    Overlap (the FP64 path's default, where the bisection is the long pole): the
+    sweep's persistent grid keeps `reserve` block slots per SM free and the
+    bisections run beside it."""
 
     def __init__(self, lib, torch, h, args, dev):
         self.lib, self.torch, self.h, self.args = lib, torch, h, args
@@ -238,27 +246,34 @@ class SweepRunner:
         if rc != 0:
             raise RuntimeError(self.lib.geon_last_error().decode())
 
+    def serial(self, precision):
+        sched = self.args.schedule
+        return precision == 1 if sched == "auto" else sched == "serial"
+
     def step(self, precision, alpha, lo, hi, r_obs=R_OBS, bisect=True, reserve=None):
         torch, lib = self.torch, self.lib
         n = alpha.numel()
+        serial = self.serial(precision) and bisect
         main = torch.cuda.current_stream()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
         ev[0].record(main)
         self.sa.wait_stream(main)
         self.sb.wait_stream(main)
-        ev[1].record(self.sa)
-        lib.geon_set_persistent_reserve_f(self.args.reserve if reserve is None else reserve)
-        self.check(lib.geon_shadow_classify_dev(self.h, r_obs, alpha.data_ptr(), n, STEP, MAX_STEPS, precision,
-                                                self.d_term.data_ptr(), self.d_steps.data_ptr(),
-                                                self.sa.cuda_stream))
-        lib.geon_set_persistent_reserve(0)
-        ev[2].record(self.sa)
         ev[3].record(self.sb)
         if bisect:
             self.check(lib.geon_shadow_bisect_dev(self.h, r_obs, lo.data_ptr(), hi.data_ptr(), lo.numel(), ITERS,
                                                   STEP, MAX_STEPS, precision, self.d_ac.data_ptr(), None, None,
                                                   self.d_bst.data_ptr(), self.sb.cuda_stream))
         ev[4].record(self.sb)
+        if serial:
+            self.sa.wait_stream(self.sb)  # the sweep after the bisection rounds, on every slot
+        ev[1].record(self.sa)
+        lib.geon_set_persistent_reserve_f(0.0 if serial else (self.args.reserve if reserve is None else reserve))
+        self.check(lib.geon_shadow_classify_dev(self.h, r_obs, alpha.data_ptr(), n, STEP, MAX_STEPS, precision,
+                                                self.d_term.data_ptr(), self.d_steps.data_ptr(),
+                                                self.sa.cuda_stream))
+        lib.geon_set_persistent_reserve(0)
+        ev[2].record(self.sa)
         main.wait_stream(self.sa)
         main.wait_stream(self.sb)
         ev[5].record(main)
@@ -282,6 +297,9 @@ def main():
     ap.add_argument("--cpu-rays", type=int, default=4096)
     ap.add_argument("--bisect-rays", type=int, default=BISECT_RAYS,
                     help="speculative bisection width (rays per round over all brackets)")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "serial", "overlap"],
+                    help="bisections before the sweep (serial: the mixed path's default) or beside it "
+                         "(overlap: the FP64 path's default)")
     ap.add_argument("--reserve", type=float, default=RESERVE,
                     help="block slots per SM the sweep leaves free for the bisections (latency vs throughput)")
     ap.add_argument("--fp64-sample", type=int, default=32, help="accuracy and FP64 legs trace every k-th sweep ray")
@@ -418,7 +436,9 @@ def main():
                                "40-iteration bisections, r_obs 20M, h 0.01, cap 200000, escape 1000M",
                    "precision": args.precision, "rays_per_gpu": N_SWEEP, "bisections_per_gpu": N_BRACKETS,
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"{world} independent shards",
-                   "sweep_reserve_blocks_per_sm": args.reserve, "bisect_rays_per_round": args.bisect_rays,
+                   "schedule": ("bisection rounds first, then the sweep on every block slot" if run.serial(prec)
+                                else f"bisections beside the sweep, {args.reserve} block slots per SM reserved"),
+                   "bisect_rays_per_round": args.bisect_rays,
                    "mixed_kernel_variant": lib.geon_get_mixed_variant(1, 1) if prec == 1 else None,
                    "mixed_block_size": (128, 64, 256)[lib.geon_get_mixed_variant(1, 1) // 3] if prec == 1 else None,
                    "sweep_claim_order": "longest first" if args.sweep_order else "index order",
