@@ -60,14 +60,14 @@ N_SWEEP = 1 << 20
 N_BRACKETS = 64
 ITERS = 40
 SCHW = [1.0, 1.001, 1000.0]
-# Slots of 128 threads per SM the persistent sweep grid leaves to the concurrent
-# bisection rounds. The bisection is a chain of dependent rounds (latency-bound),
-# the sweep throughput-bound. With the early class decision a round ends once
-# its slowest near-critical ray settles, so 2 of the 8 slots per SM keep the
-# bisections well inside the sweep (measured on GB300, sweep / bisection ms:
-# 320 / 314 at 0, 327 / 212 at 1, 326 / 97 at 2, 337 / 27 at 4, 448 / 13 at
-# 6; 2.06e11, 2.01e11, 2.02e11, 1.95e11, 1.47e11 ray-steps/s): 2 costs 1.5 %
-# of throughput against 0 and cuts the bisections' latency threefold.
+# Overlap schedule only: slots of 128 threads per SM the persistent sweep grid
+# leaves to the concurrent bisection rounds. The bisection is a chain of
+# dependent rounds (latency-bound), the sweep throughput-bound. With the early
+# class decision a round ends once its slowest near-critical ray settles, so 2
+# of the 8 slots per SM keep the bisections well inside the sweep (measured on
+# GB300, sweep / bisection ms: 320 / 314 at 0, 327 / 212 at 1, 326 / 97 at 2,
+# 337 / 27 at 4, 448 / 13 at 6). The serial schedule (the mixed path's
+# default) beats all of these: the rounds alone take 6 ms.
 RESERVE = 2
 BISECT_RAYS = 16384  # speculative width of a bisection round (geon_set_bisect_rays_per_round)
 ALG_FLOPS_PER_STEP = 268  # 4 closed-form Schwarzschild RHS (41 flops each) + 104 RK4 combine flops
