@@ -462,7 +462,7 @@ def main():
 
 def fp64_latency_leg(run, torch, flush, d_alpha, d_lo, d_hi, args, value, precision, steps):
     """An FP64 precision on the headline's kind of step: every fp64_sample-th
-    sweep ray (the whole sweep would take minutes: GB300 runs FP64 at 1/62 of
+    sweep ray (the whole sweep would take minutes: GB300 runs FP64 at ~1/60 of
     its FP32 rate) beside all 64 bisections, `steps` device-timed steps."""
     sub = d_alpha[:: max(1, args.fp64_sample)].contiguous()
     out = []
