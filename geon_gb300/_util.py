@@ -1,5 +1,4 @@
 """Shared helpers: numpy <-> ctypes, status -> exception."""
-import ctypes
 
 import numpy as np
 

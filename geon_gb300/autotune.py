@@ -9,8 +9,6 @@ import ctypes
 import json
 import os
 
-import numpy as np
-
 from . import _ffi
 from ._util import check
 

@@ -4,7 +4,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _ffi
-from ._util import check, dp, f64, i32p, i64p, points
+from ._util import check, dp, i32p, i64p, points
 
 FP64, MIXED, ADAPTIVE, FP64_FAST = 0, 1, 2, 3
 PRECISION = {"fp64": FP64, "mixed": MIXED, "adaptive": ADAPTIVE, "fp64fast": FP64_FAST,

@@ -1,7 +1,7 @@
 """render::render (render.rs:55-166) on the GPU, plus the host PNG writer."""
 import struct
 import zlib
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

@@ -5,7 +5,6 @@ Only tests/, the smoke check and bench.py's CPU-baseline leg use this module,
 and only as the checker, never as the thing measured or shipped.
 """
 import ctypes
-import os
 
 import numpy as np
 

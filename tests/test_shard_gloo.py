@@ -4,8 +4,6 @@ ranks (slowest rank's time, sum of the units), with no data-path exchange."""
 import os
 import socket
 
-import numpy as np
-import pytest
 import torch.multiprocessing as mp
 
 
